@@ -1,0 +1,387 @@
+#!/usr/bin/env python3
+"""Benchmark: batched multi-view voxel-space render on one GB300 (or N replicas).
+
+Workload (default "batch512"): 512 cameras over one shared 4096x4096 map pair
+(u8 diamond-square heights, roughness 0.55; u32 palette colours +-12 noise),
+resolutions uniform over {320x240, 640x480, 1280x720, 1920x1080, 2560x1440},
+draw distance uniform in [400, 3000], yaw uniform, height 20..200 above the
+local terrain maximum; reference-default depth schedule (d=0.001, z0=0,
+scale=w/2), bilinear height and colour. One step renders every view once with
+the persistent kernel replayed from a CUDA graph. The plain per-frame loop
+(two launches per view) is timed on the same plan for comparison.
+
+Prints one JSON line (rank 0). `value` is whole-job Gpix/s with maps resident
+in HBM; `e2e` is the same metric through the public C ABI with host buffers:
+per step the cameras go host->device and every frame device->pinned host.
+`--impl reference` times the CPU restatement of the reference path (the
+oracle, OpenMP over columns, all host threads) on a bounded sample instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+RESOLUTIONS = [(320, 240), (640, 480), (1280, 720), (1920, 1080), (2560, 1440)]
+MAP_SEED_H, MAP_SEED_C, VIEW_SEED = 7, 8, 20240601
+
+
+def batch_views(fs, hm, nviews: int, seed: int):
+    rng = np.random.default_rng(seed)
+    views = []
+    for v in range(nviews):
+        w, h = RESOLUTIONS[int(rng.integers(0, len(RESOLUTIONS)))]
+        cam = fs.gen_cameras(seed * 1000 + v, hm, 1, above=(20.0, 200.0), distance=(400.0, 3000.0),
+                             screen_h=h)[0]
+        views.append((cam, w, h))
+    return views
+
+
+def walk_views(fs, hm, seed: int):
+    return [(c, 1920, 1080) for c in fs.gen_walk(seed, hm, 64, step=2.0, yaw=0.02,
+                                                  above=(30.0, 120.0), distance=3000.0,
+                                                  screen_h=1080)]
+
+
+def make_workload(fs, name: str, rank: int):
+    if name == "batch512":
+        hm = fs.gen_heights(MAP_SEED_H, 4096, 0.55)
+        cm = fs.gen_colors(MAP_SEED_C, hm, 12)
+        return hm, cm, batch_views(fs, hm, 512, VIEW_SEED + rank), {
+            "workload": "batch512: 512 views, mixed 320x240..2560x1440, D~U[400,3000], 4096^2 maps",
+            "views": 512, "map": "4096x4096 u8 heights + u32 colours", "resolutions": RESOLUTIONS}
+    if name == "walk1080":
+        hm = fs.gen_heights(MAP_SEED_H, 4096, 0.55)
+        cm = fs.gen_colors(MAP_SEED_C, hm, 12)
+        return hm, cm, walk_views(fs, hm, 9 + rank), {
+            "workload": "walk1080: 64-frame walk, 1920x1080, D=3000, 4096^2 maps",
+            "views": 64, "map": "4096x4096 u8 heights + u32 colours"}
+    raise SystemExit(f"unknown workload {name}")
+
+
+def view_bytes(views, samples: int, events: int) -> dict:
+    frame = sum(4 * w * h for _, w, h in views)
+    return {"frame": frame, "height_gather": 4 * samples, "color_gather": 16 * events}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.t = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.t = threading.Thread(target=self._read, daemon=True)
+        self.t.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.t:
+            self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d["hbm_gbs"], "source": "measured (MEASURED_PEAKS.json)"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def profiled_traffic(name: str):
+    """DRAM bytes per launch from the committed ncu summary, if one exists."""
+    p = ROOT / "profiles" / f"render_{name}.md"
+    if not p.exists():
+        return None
+    for line in p.read_text().splitlines():
+        if line.startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_reference_rate(views, hm, cm, max_seconds: float, threads: int):
+    """Oracle (CPU restatement) Gpix/s on a bounded prefix of the views."""
+    import oracle
+    params = oracle.make_params()
+    px = 0
+    t0 = time.perf_counter()
+    used = 0
+    for cam, w, h in views:
+        oracle.render(cam, params, hm, cm, w, h, threads=threads)
+        px += w * h
+        used += 1
+        if time.perf_counter() - t0 > max_seconds:
+            break
+    dt = time.perf_counter() - t0
+    return px / dt / 1e9, used, px, dt
+
+
+def run_reference(args, rank: int, world: int):
+    if rank != 0:
+        return
+    import futspace_gb300 as fs
+    import oracle
+    hm, cm, views, cfg = make_workload(fs, args.workload, 0)
+    threads = oracle.lib().fso_max_threads()
+    rates, pxs, dts = [], 0, 0.0
+    order = list(range(len(views)))
+    for step in range(args.warmup + args.steps):
+        # each step: a bounded sample of the workload (views in a rotating order)
+        k = (step * 7) % len(views)
+        sample = [views[(k + i) % len(views)] for i in range(args.ref_views)]
+        g, used, px, dt = cpu_reference_rate(sample, hm, cm, args.ref_seconds, threads)
+        if step >= args.warmup:
+            rates.append(g)
+            pxs += px
+            dts += dt
+    value = pxs / dts / 1e9
+    line = {
+        "impl": "reference", "metric": "Gpix/s (bit-exact voxel-space frames)", "value": value,
+        "unit": "Gpix/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * dts / max(1, args.steps), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": cfg,
+        "cpu_baseline": {"value": value, "unit": "Gpix/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.ref_views} views per step of the {args.workload} "
+                                   "workload, CPU oracle (C restatement of the reference render, "
+                                   "OpenMP over columns)"},
+        "e2e": {"value": value, "unit": "Gpix/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="batch512", choices=["batch512", "walk1080"])
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--ref-views", type=int, default=4)
+    ap.add_argument("--ref-seconds", type=float, default=20.0)
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    import futspace_gb300 as fs
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    ctx = fs.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle, device=local)
+    hm, cm, views, cfg = make_workload(fs, args.workload, rank)
+    fmap = fs.Map(ctx, hm, cm)
+    plan = fs.Plan(ctx, [fmap], views)
+    tune_info = None
+    if not args.no_autotune:
+        tune_info = plan.autotune(reps=3)
+    tune = plan.get_tune()
+    px = sum(w * h for _, w, h in views)
+
+    # L2 flush buffer (larger than the 129 MB L2), written between timed steps
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device=f"cuda:{local}")
+
+    def flush_l2():
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+
+    # work counters (untimed): evaluated depth samples and coloured events
+    ctx.stats(True)
+    plan.run()
+    samples, events = ctx.stats(False)
+
+    def timed(fn, steps):
+        times = []
+        for _ in range(steps):
+            flush_l2()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            fn()
+            b.record(stream)
+            b.synchronize()
+            times.append(a.elapsed_time(b))
+        return times
+
+    for _ in range(args.warmup):
+        plan.run()
+    ctx.sync()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = ctx.launches
+    t_batch = timed(plan.run, args.steps)
+    gpu_launches = ctx.launches - launches0
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+
+    t_plain = []
+    if not args.no_plain:
+        plan.run_per_view()
+        ctx.sync()
+        t_plain = timed(plan.run_per_view, max(3, args.steps // 2))
+
+    # end to end through the C ABI: cameras host->device, render, frames -> pinned host
+    e2e = None
+    if not args.no_e2e:
+        host = torch.empty(plan.total_pixels, dtype=torch.int32, pin_memory=True)
+        cams = [v[0] for v in views]
+        t_e2e = []
+        for i in range(args.warmup + max(3, args.steps // 2)):
+            flush_l2()
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            plan.set_cameras(cams)
+            plan.run()
+            plan.download(host.numpy().view(np.uint32))
+            b.record(stream)
+            b.synchronize()
+            if i >= args.warmup:
+                t_e2e.append(a.elapsed_time(b))
+        e2e_ms = float(np.mean(t_e2e))
+        e2e = {"value": px / e2e_ms / 1e6, "unit": "Gpix/s",
+               "h2d_bytes_per_step": 96 * len(views),  # one 96-byte view record per camera
+               "d2h_bytes_per_step": 4 * plan.total_pixels,
+               "ms_per_step": e2e_ms}
+
+    ms = float(np.mean(t_batch))
+    ms_max = ms
+    if dist:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    value = px * world / ms_max / 1e6
+
+    peaks = measured_peaks()
+    vb = view_bytes(views, samples, events)
+    alg = vb["frame"] + vb["height_gather"] + vb["color_gather"]
+    achieved = alg / (ms * 1e-3) / 1e9
+    traffic = profiled_traffic(args.workload)
+
+    cpu = None
+    if rank == 0 and args.cpu_seconds > 0:
+        import oracle
+        threads = oracle.lib().fso_max_threads()
+        g, used, cpx, dt = cpu_reference_rate(views, hm, cm, args.cpu_seconds, threads)
+        cpu = {"value": g, "unit": "Gpix/s", "cores": threads, "kind": "port",
+               "sample": f"first {used} views of the workload ({cpx} px, {dt:.1f} s), CPU oracle "
+                         "(C restatement of the reference render, OpenMP over columns)"}
+
+    if rank == 0:
+        full_s = sum(fs.num_depths(v[0].distance) * v[1] for v in views)
+        line = {
+            "metric": "Gpix/s (bit-exact voxel-space frames), batched multi-view",
+            "value": value, "unit": "Gpix/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded diamond-square maps and cameras)",
+            "config": {**cfg, "l2": "flushed between timed steps (256 MB write)",
+                       "tune": {"tile_width": tune[0], "lanes_per_column": tune[1],
+                                "depth_per_lane": tune[2], "stage": tune[3],
+                                "persistent_ctas": tune[4]}},
+            "latency_ms": {"p50": float(np.percentile(t_batch, 50)),
+                           "p99": float(np.percentile(t_batch, 99))},
+            "plain_per_frame": None if not t_plain else {
+                "value": px / float(np.mean(t_plain)) / 1e6, "unit": "Gpix/s",
+                "ms_per_step": float(np.mean(t_plain)),
+                "p50_ms": float(np.percentile(t_plain, 50)),
+                "p99_ms": float(np.percentile(t_plain, 99)),
+                "launches_per_step": 2 * len(views)},
+            "batched_over_plain": None if not t_plain else float(np.mean(t_plain)) / ms,
+            "frames_per_s": len(views) * world / ms_max * 1e3,
+            "work": {"depth_samples": samples, "full_depth_samples": full_s,
+                     "events_coloured": events},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                         "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                         "traffic": traffic, "peak_source": peaks["source"],
+                         "bytes_per_step": vb},
+            "clocks": clk,
+            "e2e": e2e,
+            "gpu_launches": gpu_launches,
+            "cpu_baseline": cpu,
+        }
+        if tune_info:
+            line["config"]["autotune_ms"] = tune_info[1]
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,426 @@
+"""futspace_gb300 -- Voxel Space terrain renderer for one NVIDIA GB300 (sm_103a).
+
+Python mirror of the C ABI in include/futspace_gb300.h, over ctypes. Every
+render goes through the CUDA kernels in libfutspace_gb300.so; there is no CPU
+fallback, and importing the renderer without the built library raises.
+
+The renderer is the reference's per-frame ``render`` entry
+(fut/interactive_entrypoints.fut:19-20 -> fut/interactive.fut:173-183 ->
+fut/voxel_renderer.fut:101-251) with the samplers of
+fut/render_functions.fut:63-105.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+from typing import Iterable, Sequence
+
+import numpy as np
+
+__all__ = [
+    "FsError", "Camera", "Params", "View", "Context", "Map", "Plan", "lib", "library_path",
+    "default_params", "num_depths", "gen_heights", "gen_colors", "gen_cameras", "gen_walk",
+    "local_max", "NEAREST", "BILINEAR", "GAP_ZERO", "GAP_SKY",
+]
+
+NEAREST, BILINEAR = 0, 1
+GAP_ZERO, GAP_SKY = 0, 1
+_ERRORS = {1: "FS_ERR_ARG", 2: "FS_ERR_CUDA", 3: "FS_ERR_RANGE", 4: "FS_ERR_NOMEM",
+           5: "FS_ERR_BUDGET", 6: "FS_ERR_STATE"}
+
+
+class FsError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Camera(C.Structure):
+    """camera record, fut/voxel_renderer.fut:5-12"""
+    _fields_ = [("x", C.c_float), ("y", C.c_float), ("height", C.c_float), ("angle", C.c_float),
+                ("horizon", C.c_float), ("distance", C.c_float), ("fov", C.c_float),
+                ("sky_color", C.c_uint32)]
+
+    def as_tuple(self):
+        return tuple(getattr(self, f) for f, _ in self._fields_)
+
+
+class Params(C.Structure):
+    _fields_ = [("invz_param1", C.c_float), ("invz_param2", C.c_float),
+                ("magic_number", C.c_float), ("height_filter", C.c_int32),
+                ("color_filter", C.c_int32), ("gap_rule", C.c_int32), ("floor_n", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class View(C.Structure):
+    _fields_ = [("cam", Camera), ("width", C.c_int32), ("height", C.c_int32),
+                ("map", C.c_int32), ("reserved", C.c_int32)]
+
+
+def library_path() -> Path:
+    return Path(__file__).resolve().parent / "_lib" / "libfutspace_gb300.so"
+
+
+_LIB = None
+
+
+def _sig(lib, name, res, args):
+    f = getattr(lib, name)
+    f.restype = res
+    f.argtypes = args
+
+
+def lib():
+    """The loaded native library; raises if it has not been built."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not path.exists():
+        raise FsError(6, f"native library missing: {path} (run __graft_entry__.build())")
+    L = C.CDLL(str(path))
+    vp, i32, i64, u64, f32 = C.c_void_p, C.c_int32, C.c_int64, C.c_uint64, C.c_float
+    P = C.POINTER
+    _sig(L, "fs_params_default", Params, [])
+    _sig(L, "fs_ctx_new", C.c_int, [P(vp), i32])
+    _sig(L, "fs_ctx_free", None, [vp])
+    _sig(L, "fs_ctx_get_error", vp, [vp])
+    _sig(L, "fs_ctx_sync", C.c_int, [vp])
+    _sig(L, "fs_ctx_set_stream", C.c_int, [vp, vp])
+    _sig(L, "fs_ctx_get_stream", vp, [vp])
+    _sig(L, "fs_ctx_kernel_launches", i64, [vp])
+    _sig(L, "fs_ctx_stats", C.c_int, [vp, i32, P(u64)])
+    _sig(L, "fs_ctx_force_tune", C.c_int, [vp, P(i32)])
+    _sig(L, "fs_map_new", C.c_int, [vp, P(vp), vp, vp, i64, i64])
+    _sig(L, "fs_map_new_i32", C.c_int, [vp, P(vp), vp, vp, i64, i64])
+    _sig(L, "fs_map_wrap_device", C.c_int, [vp, P(vp), vp, vp, i64, i64])
+    _sig(L, "fs_map_free", C.c_int, [vp, vp])
+    _sig(L, "fs_map_shape", C.c_int, [vp, P(i64), P(i64)])
+    _sig(L, "fs_map_quads_dev", vp, [vp])
+    _sig(L, "fs_map_colors_dev", vp, [vp])
+    _sig(L, "fs_num_depths", i32, [f32, P(Params)])
+    _sig(L, "fs_render_device", C.c_int, [vp, vp, P(Camera), P(Params), i32, i32, vp])
+    _sig(L, "fs_render", C.c_int, [vp, vp, P(Camera), P(Params), i32, i32, vp])
+    _sig(L, "fs_plan_new", C.c_int, [vp, P(vp), P(vp), i32, P(Params), P(View), i32])
+    _sig(L, "fs_plan_free", None, [vp])
+    _sig(L, "fs_plan_set_cameras", C.c_int, [vp, P(Camera), i32])
+    _sig(L, "fs_plan_run", C.c_int, [vp])
+    _sig(L, "fs_plan_run_per_view", C.c_int, [vp])
+    _sig(L, "fs_plan_frame_dev", vp, [vp, i32])
+    _sig(L, "fs_plan_frame_offset", i64, [vp, i32])
+    _sig(L, "fs_plan_total_pixels", i64, [vp])
+    _sig(L, "fs_plan_download", C.c_int, [vp, vp])
+    _sig(L, "fs_plan_get_tune", C.c_int, [vp, P(i32)])
+    _sig(L, "fs_plan_set_tune", C.c_int, [vp, P(i32)])
+    _sig(L, "fs_plan_signature", C.c_int, [vp, P(i64)])
+    _sig(L, "fs_autotune_frame", C.c_int,
+         [vp, vp, P(Camera), P(Params), i32, i32, i32, P(i32), P(f32)])
+    _sig(L, "fs_plan_autotune", C.c_int, [vp, i32, P(i32), P(f32)])
+    _sig(L, "fs_tune_count", C.c_int, [])
+    _sig(L, "fs_tune_get", C.c_int, [C.c_int, P(i32)])
+    _sig(L, "fsgen_heights", C.c_int, [u64, i32, f32, vp])
+    _sig(L, "fsgen_colors", C.c_int, [u64, vp, i64, i32, vp])
+    _sig(L, "fsgen_local_max", i32, [vp, i32, i32, f32, f32])
+    _sig(L, "fsgen_cameras", C.c_int,
+         [u64, vp, i32, i32, i32, f32, f32, f32, f32, i32, P(Camera)])
+    _sig(L, "fsgen_walk", C.c_int,
+         [u64, vp, i32, i32, i32, f32, f32, f32, f32, f32, i32, P(Camera)])
+    _LIB = L
+    return L
+
+
+def _ptr(a) -> int:
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return int(a)
+
+
+def default_params(**kw) -> Params:
+    p = lib().fs_params_default()
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def num_depths(distance: float, params: Params | None = None) -> int:
+    return lib().fs_num_depths(float(distance), C.byref(params or default_params()))
+
+
+# ---- synthetic inputs -----------------------------------------------------------------
+
+def _check(rc: int, what: str):
+    if rc != 0:
+        raise FsError(rc, what)
+
+
+def gen_heights(seed: int, size: int, roughness: float = 0.55) -> np.ndarray:
+    out = np.empty((size, size), np.uint8)
+    _check(lib().fsgen_heights(seed, size, roughness, _ptr(out)), "fsgen_heights")
+    return out
+
+
+def gen_colors(seed: int, heights: np.ndarray, noise: int = 12) -> np.ndarray:
+    h = np.ascontiguousarray(heights, np.uint8)
+    out = np.empty(h.shape, np.uint32)
+    _check(lib().fsgen_colors(seed, _ptr(h), h.size, noise, _ptr(out)), "fsgen_colors")
+    return out
+
+
+def local_max(heights: np.ndarray, x: float, y: float) -> int:
+    h = np.ascontiguousarray(heights, np.uint8)
+    return lib().fsgen_local_max(_ptr(h), h.shape[0], h.shape[1], x, y)
+
+
+def gen_cameras(seed: int, heights: np.ndarray, count: int, above=(40.0, 40.0),
+                distance=(800.0, 800.0), screen_h: int = 240) -> list[Camera]:
+    h = np.ascontiguousarray(heights, np.uint8)
+    arr = (Camera * count)()
+    _check(lib().fsgen_cameras(seed, _ptr(h), h.shape[0], h.shape[1], count, above[0], above[1],
+                               distance[0], distance[1], screen_h, arr), "fsgen_cameras")
+    return list(arr)
+
+
+def gen_walk(seed: int, heights: np.ndarray, count: int, step: float = 2.0, yaw: float = 0.02,
+             above=(30.0, 120.0), distance: float = 3000.0, screen_h: int = 1080) -> list[Camera]:
+    h = np.ascontiguousarray(heights, np.uint8)
+    arr = (Camera * count)()
+    _check(lib().fsgen_walk(seed, _ptr(h), h.shape[0], h.shape[1], count, step, yaw, above[0],
+                            above[1], distance, screen_h, arr), "fsgen_walk")
+    return list(arr)
+
+
+# ---- objects ---------------------------------------------------------------------------
+
+class Context:
+    """fs_ctx: one device, one stream, error text, scratch buffers."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        rc = lib().fs_ctx_new(C.byref(self._h), device)
+        if rc != 0:
+            msg = self.error() if self._h else "fs_ctx_new"
+            if self._h:
+                lib().fs_ctx_free(self._h)
+                self._h = C.c_void_p()
+            raise FsError(rc, msg or "fs_ctx_new")
+
+    @property
+    def handle(self):
+        return self._h
+
+    def error(self) -> str:
+        p = lib().fs_ctx_get_error(self._h)
+        if not p:
+            return ""
+        s = C.string_at(p).decode()
+        C.CDLL(None).free(C.c_void_p(p))
+        return s
+
+    def check(self, rc: int, what: str):
+        if rc != 0:
+            raise FsError(rc, f"{what}: {self.error()}")
+
+    def sync(self):
+        self.check(lib().fs_ctx_sync(self._h), "sync")
+
+    def set_stream(self, stream_handle: int | None):
+        self.check(lib().fs_ctx_set_stream(self._h, stream_handle or None), "set_stream")
+
+    @property
+    def stream_handle(self) -> int:
+        """The cudaStream_t every asynchronous call of this context uses."""
+        return lib().fs_ctx_get_stream(self._h) or 0
+
+    @property
+    def launches(self) -> int:
+        return lib().fs_ctx_kernel_launches(self._h)
+
+    def force_tune(self, tune=None):
+        """tune = (tile_width, lanes_per_column, depth_per_lane, stage) or None."""
+        t = (C.c_int32 * 5)(*(tuple(tune) + (0,) * (5 - len(tune)))) if tune else None
+        self.check(lib().fs_ctx_force_tune(self._h, t), "force_tune")
+
+    def stats(self, enable: bool = True):
+        out = (C.c_uint64 * 2)()
+        self.check(lib().fs_ctx_stats(self._h, int(enable), out), "stats")
+        return int(out[0]), int(out[1])
+
+    def close(self):
+        if self._h:
+            lib().fs_ctx_free(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- renders --
+    def render(self, fmap: "Map", cam: Camera, width: int, height: int,
+               params: Params | None = None, out: np.ndarray | None = None) -> np.ndarray:
+        """Plain per-frame render into host memory ([height][width] u32 ARGB)."""
+        if out is None:
+            out = np.empty((height, width), np.uint32)
+        assert out.dtype == np.uint32 and out.flags.c_contiguous and out.size == width * height
+        self.check(lib().fs_render(self._h, fmap.handle, C.byref(cam),
+                                   C.byref(params or default_params()), width, height, _ptr(out)),
+                   "fs_render")
+        return out
+
+    def render_device(self, fmap: "Map", cam: Camera, width: int, height: int, out_dev,
+                      params: Params | None = None):
+        """Asynchronous render into device memory (pointer or tensor with data_ptr)."""
+        self.check(lib().fs_render_device(self._h, fmap.handle, C.byref(cam),
+                                          C.byref(params or default_params()), width, height,
+                                          _ptr(out_dev)), "fs_render_device")
+
+    def autotune_frame(self, fmap: "Map", cam: Camera, width: int, height: int,
+                       params: Params | None = None, reps: int = 5):
+        out = (C.c_int32 * 5)()
+        ms = C.c_float()
+        self.check(lib().fs_autotune_frame(self._h, fmap.handle, C.byref(cam),
+                                           C.byref(params or default_params()), width, height,
+                                           reps, out, C.byref(ms)), "autotune_frame")
+        return tuple(out[:4]), ms.value
+
+
+class Map:
+    """fs_map: a resident height/colour map pair."""
+
+    def __init__(self, ctx: Context, heights: np.ndarray, colors: np.ndarray):
+        self.ctx = ctx
+        self._h = C.c_void_p()
+        assert heights.shape == colors.shape and heights.ndim == 2
+        if heights.dtype == np.int32:
+            h = np.ascontiguousarray(heights)
+            fn = lib().fs_map_new_i32
+        else:
+            h = np.ascontiguousarray(heights, np.uint8)
+            fn = lib().fs_map_new
+        c = np.ascontiguousarray(colors, np.uint32)
+        ctx.check(fn(ctx.handle, C.byref(self._h), _ptr(h), _ptr(c), h.shape[0], h.shape[1]),
+                  "fs_map_new")
+        self.shape = h.shape
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            lib().fs_map_free(self.ctx.handle, self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Plan:
+    """fs_plan: batched multi-view render (persistent kernel, CUDA graph)."""
+
+    def __init__(self, ctx: Context, maps: Sequence[Map], views: Sequence[tuple],
+                 params: Params | None = None):
+        """views: (Camera, width, height[, map_index]) tuples."""
+        self.ctx = ctx
+        self._h = C.c_void_p()
+        arr = (View * len(views))()
+        for i, v in enumerate(views):
+            arr[i].cam = v[0]
+            arr[i].width = v[1]
+            arr[i].height = v[2]
+            arr[i].map = v[3] if len(v) > 3 else 0
+        mp = (C.c_void_p * len(maps))(*[m.handle.value for m in maps])
+        self.params = params or default_params()
+        ctx.check(lib().fs_plan_new(ctx.handle, C.byref(self._h), mp, len(maps),
+                                    C.byref(self.params), arr, len(views)), "fs_plan_new")
+        self.sizes = [(v[1], v[2]) for v in views]
+        self.nviews = len(views)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def run(self):
+        self.ctx.check(lib().fs_plan_run(self._h), "fs_plan_run")
+
+    def run_per_view(self):
+        self.ctx.check(lib().fs_plan_run_per_view(self._h), "fs_plan_run_per_view")
+
+    def set_cameras(self, cams: Iterable[Camera]):
+        cams = list(cams)
+        arr = (Camera * len(cams))(*cams)
+        self.ctx.check(lib().fs_plan_set_cameras(self._h, arr, len(cams)), "set_cameras")
+
+    @property
+    def total_pixels(self) -> int:
+        return lib().fs_plan_total_pixels(self._h)
+
+    def frame_offset(self, i: int) -> int:
+        return lib().fs_plan_frame_offset(self._h, i)
+
+    def frame_dev(self, i: int) -> int:
+        return lib().fs_plan_frame_dev(self._h, i)
+
+    def download(self, out: np.ndarray | None = None) -> np.ndarray:
+        if out is None:
+            out = np.empty(self.total_pixels, np.uint32)
+        self.ctx.check(lib().fs_plan_download(self._h, _ptr(out)), "fs_plan_download")
+        return out
+
+    def frames(self, flat: np.ndarray | None = None) -> list[np.ndarray]:
+        flat = self.download() if flat is None else flat
+        res = []
+        for i, (w, h) in enumerate(self.sizes):
+            o = self.frame_offset(i)
+            res.append(flat[o:o + w * h].reshape(h, w))
+        return res
+
+    def get_tune(self):
+        """(tile_width, lanes_per_column, depth_per_lane, stage, persistent_ctas)"""
+        out = (C.c_int32 * 5)()
+        self.ctx.check(lib().fs_plan_get_tune(self._h, out), "get_tune")
+        return tuple(out)
+
+    def set_tune(self, tw: int, lc: int, u: int, stage: int = 1, ctas: int = 0):
+        t = (C.c_int32 * 5)(tw, lc, u, stage, ctas)
+        self.ctx.check(lib().fs_plan_set_tune(self._h, t), "set_tune")
+
+    def autotune(self, reps: int = 3):
+        out = (C.c_int32 * 5)()
+        ms = C.c_float()
+        self.ctx.check(lib().fs_plan_autotune(self._h, reps, out, C.byref(ms)), "autotune")
+        return tuple(out), ms.value
+
+    def close(self):
+        if self._h:
+            lib().fs_plan_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def tune_table() -> list[tuple[int, int, int, int]]:
+    """Compiled kernel configurations (tile_width, lanes_per_column, depth_per_lane, stage)."""
+    L = lib()
+    out = []
+    for i in range(L.fs_tune_count()):
+        t = (C.c_int32 * 5)()
+        L.fs_tune_get(i, t)
+        out.append(tuple(t[:4]))
+    return out

@@ -1,0 +1,100 @@
+/*
+ * Internal types shared by the C host code (fs_host.c, fs_serve.c) and the CUDA
+ * kernels (fs_kernels.cu). Plain C11 layout: no C++ in here.
+ */
+#ifndef FS_INTERNAL_H
+#define FS_INTERNAL_H
+
+#include <cuda.h>
+#include <cuda_runtime_api.h>
+#include <stdint.h>
+
+#include "../../include/futspace_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Largest screen height the column stage supports (rows are packed in 16 bits
+ * in the per-warp event queues). */
+#define FS_MAX_ROWS 16383
+/* Largest depth-sample count per view (depth index packed in 20 bits). */
+#define FS_MAX_DEPTHS (1 << 20)
+/* Maps bound to one launch. */
+#define FS_MAX_MAPS 4
+
+/* Filter flags of a view. */
+#define FSV_HEIGHT_BILINEAR 1
+#define FSV_COLOR_BILINEAR 2
+
+/* One view (camera + screen) as the kernels read it. 96 bytes. */
+typedef struct {
+  float cam_x, cam_y, cam_h, horizon;
+  float sa, ca, fov, scale; /* sin/cos of the yaw from the host C library */
+  float d, z0;
+  int32_t W, H;
+  int32_t n, map;
+  uint32_t sky, gap;
+  uint32_t *out;    /* frame base in device memory, row-major H x W */
+  int64_t zoff;     /* first z-table entry of this view */
+  int32_t tmap;     /* index into the tensor-map array, -1: plain stores */
+  int32_t flags;    /* FSV_* */
+  int32_t pad[2];
+} FsView;
+
+/* One height/colour map pair resident in device memory. Heights are stored as
+ * 2x2 quads: q[y][x] packs the u8 heights of (y,x), (y,x+1), (y+1,x) and
+ * (y+1,x+1) (indices wrapped) in bytes 0..3, so one 4-byte gather yields the
+ * whole bilinear footprint; byte 0 alone is the nearest sample. */
+typedef struct {
+  const uint32_t *q;  /* [MH][MW] height quads */
+  const uint32_t *c;  /* [MH][MW] ARGB colours */
+  int32_t MH, MW;
+  int32_t pow2;       /* both sizes powers of two: wrap with a mask */
+  int32_t pad;
+} FsMapDev;
+
+/* Everything one render launch needs, passed by value (__grid_constant__), so
+ * a single-view launch touches no host-written device memory. */
+typedef struct {
+  CUtensorMap tmap0;           /* frame tensor map of view0 (when tmap == 0 and views == NULL) */
+  FsView view0;                /* the view when views == NULL */
+  FsMapDev maps[FS_MAX_MAPS];
+  const FsView *views;         /* NULL: single view0 */
+  const int32_t *items;        /* work items, (view << 12) | tile; NULL: item = tile of view0 */
+  const CUtensorMap *tmaps;    /* tensor maps of `views` */
+  const float4 *zline;         /* per depth: x0, y0, dx, dy */
+  const float *zinvz;          /* per depth: inv_z */
+  int32_t *head;               /* persistent work counter; NULL: one item per CTA */
+  unsigned long long *stats;   /* optional counters: samples, events; NULL: off */
+  int32_t nitems;
+  int32_t stride_max;          /* stage column stride (>= max H, odd) */
+  int32_t pad[2];
+} FsLaunch;
+
+/* Launch configuration of the render kernel (the autotuned knobs). */
+typedef struct {
+  int32_t tw;    /* column-tile width: columns per CTA */
+  int32_t lc;    /* lanes per column (32: one warp per column) */
+  int32_t u;     /* depth samples per lane per chunk: chunk = lc * u depths */
+  int32_t stage; /* 1: shared-memory column stage + TMA store; 0: direct painting */
+  int32_t ctas;  /* persistent CTAs (0: as many as fit) */
+} FsTune;
+
+/* Kernel-side entry points (fs_kernels.cu). Each returns a cudaError_t. */
+int fsk_ztable(const FsView *views_dev, const FsView *view0, int32_t nviews, int32_t max_n,
+               float4 *zline, float *zinvz, cudaStream_t st);
+int fsk_render(const FsLaunch *L, const FsTune *t, int32_t hf, int32_t cf, int32_t grid,
+               cudaStream_t st);
+size_t fsk_render_smem(const FsTune *t, int32_t stride_max);
+int fsk_render_max_ctas_per_sm(const FsTune *t, int32_t hf, int32_t cf, int32_t stride_max,
+                               int32_t *out);
+int fsk_tune_supported(const FsTune *t);
+int fsk_shadowmap(const FsMapDev *map, const float sun[3], uint32_t *out, cudaStream_t st);
+int fsk_mask_heights(const int32_t *in, uint8_t *out, int64_t count, cudaStream_t st);
+int fsk_build_quads(const uint8_t *h, uint32_t *q, int32_t MH, int32_t MW, cudaStream_t st);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

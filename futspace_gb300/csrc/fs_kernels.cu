@@ -1,0 +1,178 @@
+/*
+ * Small kernels around the renderer and the host-facing launch wrappers:
+ *  - the per-view depth table (get_zs + get_h_line + inv_z, once per depth),
+ *  - the shadowed-colour precompute of update_map,
+ *  - the i32 -> u8 height mask of update_map,
+ *  - dispatch of the render kernel over the four filter pairs.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include "fs_device.cuh"
+#include "fs_render.cuh"
+
+using namespace fsd;
+
+extern "C" int fsk_render_h0c0(int, const FsLaunch *, const FsTune *, int, size_t, cudaStream_t,
+                               int *);
+extern "C" int fsk_render_h0c1(int, const FsLaunch *, const FsTune *, int, size_t, cudaStream_t,
+                               int *);
+extern "C" int fsk_render_h1c0(int, const FsLaunch *, const FsTune *, int, size_t, cudaStream_t,
+                               int *);
+extern "C" int fsk_render_h1c1(int, const FsLaunch *, const FsTune *, int, size_t, cudaStream_t,
+                               int *);
+
+namespace {
+
+/* Per depth k (z = z_{k+1}): get_zs (fut/voxel_renderer.fut:34), get_h_line
+ * (:43-60) and inv_z = (1/z) * scale (:217). The reference evaluates these once
+ * per depth slice in its outer map (:215-217); so does this table. */
+__global__ void ztable_kernel(const FsView *views, FsView view0, float4 *zline, float *zinvz) {
+  const FsView *Vp = views ? views + blockIdx.y : &view0;
+  const int n = Vp->n;
+  const float d = Vp->d, z0 = Vp->z0, s = Vp->sa, c = Vp->ca, v = Vp->fov;
+  const float fw = (float)Vp->W;
+  const float a1 = fs(-c, fm(s, v)); /* left_x / z  */
+  const float a2 = fs(s, fm(c, v));  /* left_y / z  */
+  const float a3 = fs(c, fm(s, v));  /* right_x / z */
+  const float a4 = fs(-s, fm(c, v)); /* right_y / z */
+  float4 *zl = zline + Vp->zoff;
+  float *zi = zinvz + Vp->zoff;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+    const float fi = (float)(k + 1);
+    const float z = fm(fd(fi, 2.0f), fa(fm(2.0f, z0), fm(fs(fi, 1.0f), d)));
+    const float lx = fm(a1, z), ly = fm(a2, z), rx = fm(a3, z), ry = fm(a4, z);
+    const float dx = fd(fs(rx, lx), fw);
+    const float dy = fd(fs(ry, ly), fw);
+    zl[k] = make_float4(fa(lx, Vp->cam_x), fa(ly, Vp->cam_y), dx, dy);
+    zi[k] = fm(fd(1.0f, z), Vp->scale);
+  }
+}
+
+/* generate_shadowmap_accumulated, fut/effects.fut:108-125, with the nearest
+ * samplers of update_map (fut/interactive.fut:344-346). 1024x1024 output. */
+__global__ void shadow_kernel(FsMapDev M, float s0, float s1, float s2, uint32_t *out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  const int y = blockIdx.y;
+  if (x >= 1024 || y >= 1024) return;
+  const float fx = (float)x, fy = (float)y;
+  const float step_size = 4.0f; /* f32(1024 / 256) */
+  const float height = height_nearest(M, fx, fy);
+  int count = 0;
+  for (int dist = 1; dist < 256; dist++) {
+    const float t = fm((float)dist, step_size);
+    const float hx = fa(fx, fm(t, s0));
+    const float hy = fa(fy, fm(t, s2));
+    const float lhs = fs(fa(height, fm(t, s1)), height_nearest(M, hx, hy));
+    if (lhs < -0.5f) count += 1;
+  }
+  const uint32_t black = 0xFF000000u; /* argb.black = from_rgba 0 0 0 1 */
+  const Channels ch{nullptr};
+  out[(size_t)y * 1024 + x] = mix(ch, fm(step_size, (float)count), black, 1.0f,
+                                  color_nearest(M, fx, fy));
+}
+
+__global__ void mask_kernel(const int32_t *in, uint8_t *out, int64_t count) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count;
+       i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (uint8_t)(in[i] & 0xFF);
+}
+
+int queue_cap(int u) {
+  const int raw = 31 + 32 * u;
+  return raw <= 64 ? 64 : (raw <= 128 ? 128 : (raw <= 256 ? 256 : 512));
+}
+
+/* Height quads: q[y][x] = h[y][x] | h[y][x+1] << 8 | h[y+1][x] << 16 |
+ * h[y+1][x+1] << 24, indices wrapped with Futhark's floored `%`. */
+__global__ void quad_kernel(const uint8_t *h, uint32_t *q, int MH, int MW) {
+  const int y = blockIdx.y;
+  const int y1 = (y + 1) % MH;
+  const uint8_t *r0 = h + (size_t)y * MW;
+  const uint8_t *r1 = h + (size_t)y1 * MW;
+  for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < MW; x += gridDim.x * blockDim.x) {
+    const int x1 = (x + 1) % MW;
+    q[(size_t)y * MW + x] = (uint32_t)r0[x] | ((uint32_t)r0[x1] << 8) | ((uint32_t)r1[x] << 16) |
+                            ((uint32_t)r1[x1] << 24);
+  }
+}
+
+typedef int (*render_entry)(int, const FsLaunch *, const FsTune *, int, size_t, cudaStream_t,
+                            int *);
+
+render_entry pick(int hf, int cf) {
+  if (hf) return cf ? fsk_render_h1c1 : fsk_render_h1c0;
+  return cf ? fsk_render_h0c1 : fsk_render_h0c0;
+}
+
+}  // namespace
+
+extern "C" int fsk_ztable(const FsView *views_dev, const FsView *view0, int32_t nviews,
+                          int32_t max_n, float4 *zline, float *zinvz, cudaStream_t st) {
+  if (nviews <= 0 || max_n <= 0) return (int)cudaSuccess;
+  const int threads = 256;
+  int bx = (max_n + threads - 1) / threads;
+  if (bx > 64) bx = 64;
+  FsView v0;
+  if (view0) v0 = *view0;
+  else memset(&v0, 0, sizeof(v0));
+  dim3 grid(bx, views_dev ? nviews : 1);
+  ztable_kernel<<<grid, threads, 0, st>>>(views_dev, v0, zline, zinvz);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int fsk_tune_supported(const FsTune *t) {
+#define FS_CASE(TW_, LC_, U_, STG_) \
+  if (t->tw == TW_ && t->lc == LC_ && t->u == U_ && t->stage == STG_) return 1;
+  FS_TUNE_LIST(FS_CASE)
+#undef FS_CASE
+  return 0;
+}
+
+extern "C" size_t fsk_render_smem(const FsTune *t, int32_t stride_max) {
+  /* must match RenderShape<...>::fixed_bytes + stage */
+  const size_t nw = (size_t)t->tw * t->lc / 32;
+  const size_t box = t->stage ? 2ull * kBoxRows * t->tw * 4 : 0;
+  const size_t stage = t->stage ? (size_t)t->tw * stride_max * 4 : 0;
+  return box + nw * queue_cap(t->u) * 8 + 256 * 4 + (size_t)t->tw * 8 + stage;
+}
+
+extern "C" int fsk_build_quads(const uint8_t *h, uint32_t *q, int32_t MH, int32_t MW,
+                               cudaStream_t st) {
+  if (MH <= 0 || MW <= 0) return (int)cudaErrorInvalidValue;
+  int bx = (MW + 255) / 256;
+  if (bx > 16) bx = 16;
+  quad_kernel<<<dim3(bx, MH), 256, 0, st>>>(h, q, MH, MW);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int fsk_render(const FsLaunch *L, const FsTune *t, int32_t hf, int32_t cf,
+                          int32_t grid, cudaStream_t st) {
+  if (grid <= 0) return (int)cudaSuccess;
+  return pick(hf, cf)(0, L, t, grid, fsk_render_smem(t, L->stride_max), st, nullptr);
+}
+
+extern "C" int fsk_render_max_ctas_per_sm(const FsTune *t, int32_t hf, int32_t cf,
+                                          int32_t stride_max, int32_t *out) {
+  int occ = 0;
+  const int e = pick(hf, cf)(1, nullptr, t, 0, fsk_render_smem(t, stride_max), 0, &occ);
+  *out = occ;
+  return e;
+}
+
+extern "C" int fsk_shadowmap(const FsMapDev *map, const float sun[3], uint32_t *out,
+                             cudaStream_t st) {
+  dim3 grid(1024 / 128, 1024);
+  shadow_kernel<<<grid, 128, 0, st>>>(*map, sun[0], sun[1], sun[2], out);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int fsk_mask_heights(const int32_t *in, uint8_t *out, int64_t count,
+                                cudaStream_t st) {
+  if (count <= 0) return (int)cudaSuccess;
+  int64_t blocks = (count + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  mask_kernel<<<(int)blocks, 256, 0, st>>>(in, out, count);
+  return (int)cudaGetLastError();
+}

@@ -1,0 +1,367 @@
+/*
+ * Batched multi-view rendering. A plan owns one framebuffer arena with a frame
+ * per view, a depth table per view, the tensor maps of the frames and a list of
+ * (view, column-tile) work items sorted by estimated cost. One run is three
+ * stream operations -- reset the work counter, build every view's depth table,
+ * launch the persistent render kernel sized to fill the GPU -- captured once
+ * into a CUDA graph and replayed. The items are pulled from the counter in
+ * cost order, so large and small views balance across the SMs.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "fs_internal.h"
+#include "fs_priv.h"
+
+typedef struct {
+  int64_t cost;
+  int32_t item;
+} fs_item_cost;
+
+static int cmp_cost_desc(const void *a, const void *b) {
+  const fs_item_cost *x = (const fs_item_cost *)a, *y = (const fs_item_cost *)b;
+  if (x->cost != y->cost) return x->cost > y->cost ? -1 : 1;
+  return x->item < y->item ? -1 : (x->item > y->item);
+}
+
+static void plan_release_graph(fs_plan *p) {
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  p->exec = NULL;
+  p->graph = NULL;
+  p->graph_ok = 0;
+}
+
+void fs_plan_free(fs_plan *p) {
+  if (!p) return;
+  cudaSetDevice(p->ctx->device);
+  cudaStreamSynchronize(p->ctx->stream);
+  plan_release_graph(p);
+  cudaFree(p->fv_d);
+  cudaFree(p->tm_d);
+  cudaFree(p->items_d);
+  cudaFree(p->head_d);
+  cudaFree(p->zline);
+  cudaFree(p->zinvz);
+  cudaFree(p->frames);
+  free(p->views_h);
+  free(p->fv_h);
+  free(p->ncap);
+  free(p->tm_h);
+  free(p->offsets);
+  free(p);
+}
+
+static void plan_fill_launch(fs_plan *p, FsLaunch *L) {
+  memset(L, 0, sizeof(*L));
+  for (int i = 0; i < p->nmaps; i++) L->maps[i] = p->maps[i];
+  L->views = p->fv_d;
+  L->items = p->items_d;
+  L->tmaps = p->tm_d;
+  L->zline = p->zline;
+  L->zinvz = p->zinvz;
+  L->head = p->head_d;
+  L->nitems = p->nitems;
+  L->stride_max = p->stride_max;
+  L->stats = p->ctx->stats_dev;
+}
+
+static int plan_enqueue(fs_plan *p) {
+  fs_ctx *ctx = p->ctx;
+  FsLaunch launch;
+  plan_fill_launch(p, &launch);
+  int32_t max_n = 0;
+  for (int v = 0; v < p->nviews; v++)
+    if (p->ncap[v] > max_n) max_n = p->ncap[v];
+  int e = cudaMemsetAsync(p->head_d, 0, sizeof(int32_t), ctx->stream);
+  if (e) return fs_cuda_fail(ctx, e, "work counter reset");
+  e = fsk_ztable(p->fv_d, NULL, p->nviews, max_n, p->zline, p->zinvz, ctx->stream);
+  if (e) return fs_cuda_fail(ctx, e, "z-table kernel launch");
+  e = fsk_render(&launch, &p->tune, p->hf, p->cf, p->grid, ctx->stream);
+  if (e) return fs_cuda_fail(ctx, e, "persistent render kernel launch");
+  return FS_OK;
+}
+
+/* (Re)builds everything that depends on the tuning: tensor maps (box width),
+ * work items (tile width), grid size and the captured graph. */
+static int plan_build(fs_plan *p) {
+  fs_ctx *ctx = p->ctx;
+  const int32_t tw = p->tune.tw;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  plan_release_graph(p);
+  int64_t nitems = 0;
+  for (int v = 0; v < p->nviews; v++) {
+    FsView *fv = &p->fv_h[v];
+    fv->out = p->frames + p->offsets[v];
+    fv->tmap = fs_encode_frame_map(ctx, fv->out, fv->W, fv->H, tw, &p->tm_h[v]) ? v : -1;
+    const int32_t tiles = (fv->W + tw - 1) / tw;
+    if (tiles > 4096) return fs_fail(ctx, FS_ERR_ARG, "view %d: too many column tiles", v);
+    nitems += tiles;
+  }
+  fs_item_cost *ic = (fs_item_cost *)malloc(sizeof(fs_item_cost) * (size_t)nitems);
+  int32_t *items = (int32_t *)malloc(sizeof(int32_t) * (size_t)nitems);
+  if (!ic || !items) {
+    free(ic);
+    free(items);
+    return fs_fail(ctx, FS_ERR_NOMEM, "malloc(items)");
+  }
+  int64_t k = 0;
+  for (int v = 0; v < p->nviews; v++) {
+    const FsView *fv = &p->fv_h[v];
+    const int32_t tiles = (fv->W + tw - 1) / tw;
+    for (int t = 0; t < tiles; t++) {
+      ic[k].cost = (int64_t)fv->n * 8 + fv->H; /* depth march dominates, then the store */
+      ic[k].item = (v << 12) | t;
+      k++;
+    }
+  }
+  qsort(ic, (size_t)nitems, sizeof(fs_item_cost), cmp_cost_desc);
+  for (int64_t i = 0; i < nitems; i++) items[i] = ic[i].item;
+  free(ic);
+  cudaFree(p->items_d);
+  p->items_d = NULL;
+  int e = cudaMalloc((void **)&p->items_d, sizeof(int32_t) * (size_t)nitems);
+  if (!e) e = cudaMemcpy(p->items_d, items, sizeof(int32_t) * (size_t)nitems,
+                         cudaMemcpyHostToDevice);
+  free(items);
+  if (e) return fs_cuda_fail(ctx, e, "items upload");
+  p->nitems = (int32_t)nitems;
+  e = cudaMemcpy(p->fv_d, p->fv_h, sizeof(FsView) * (size_t)p->nviews, cudaMemcpyHostToDevice);
+  if (!e && p->tm_d)
+    e = cudaMemcpy(p->tm_d, p->tm_h, sizeof(CUtensorMap) * (size_t)p->nviews,
+                   cudaMemcpyHostToDevice);
+  if (e) return fs_cuda_fail(ctx, e, "view upload");
+  int32_t occ = 0;
+  e = fsk_render_max_ctas_per_sm(&p->tune, p->hf, p->cf, p->stride_max, &occ);
+  if (e) return fs_cuda_fail(ctx, e, "occupancy query");
+  if (occ < 1) return fs_fail(ctx, FS_ERR_ARG, "render kernel does not fit on an SM");
+  int64_t grid = (int64_t)occ * ctx->sm_count;
+  if (p->tune.ctas > 0 && p->tune.ctas < grid) grid = p->tune.ctas;
+  if (grid > nitems) grid = nitems;
+  p->grid = (int32_t)grid;
+
+  /* capture reset + depth tables + persistent render into one graph */
+  e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
+  if (e) return fs_cuda_fail(ctx, e, "cudaStreamBeginCapture");
+  int rc = plan_enqueue(p);
+  cudaGraph_t g = NULL;
+  e = cudaStreamEndCapture(ctx->stream, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e) return fs_cuda_fail(ctx, e, "cudaStreamEndCapture");
+  p->graph = g;
+  e = cudaGraphInstantiate(&p->exec, g, 0);
+  if (e) return fs_cuda_fail(ctx, e, "cudaGraphInstantiate");
+  p->graph_ok = 1;
+  return FS_OK;
+}
+
+static int64_t batch_signature(const fs_plan *p) {
+  /* order-independent hash of the (W, H) multiset */
+  uint64_t h = 0;
+  for (int v = 0; v < p->nviews; v++) {
+    uint64_t x = ((uint64_t)(uint32_t)p->fv_h[v].W << 32) | (uint32_t)p->fv_h[v].H;
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdULL;
+    x ^= x >> 33;
+    h += x;
+  }
+  return (int64_t)(h ^ (uint64_t)p->nviews);
+}
+
+int fs_plan_signature(const fs_plan *p, int64_t *sig) {
+  if (!p || !sig) return FS_ERR_ARG;
+  *sig = batch_signature(p);
+  return FS_OK;
+}
+
+int fs_plan_new(fs_ctx *ctx, fs_plan **out, const fs_map *const *maps, int32_t nmaps,
+                const fs_params *params, const fs_view *views, int32_t nviews) {
+  if (!ctx || !out) return FS_ERR_ARG;
+  *out = NULL;
+  if (ctx->broken) return fs_fail(ctx, FS_ERR_STATE, "context failed to initialise");
+  if (!maps || nmaps < 1 || nmaps > FS_MAX_MAPS)
+    return fs_fail(ctx, FS_ERR_ARG, "need 1..%d maps", FS_MAX_MAPS);
+  if (!views || nviews < 1 || nviews >= (1 << 19))
+    return fs_fail(ctx, FS_ERR_ARG, "need 1..%d views", (1 << 19) - 1);
+  for (int i = 0; i < nmaps; i++)
+    if (!maps[i]) return fs_fail(ctx, FS_ERR_ARG, "map %d is NULL", i);
+  fs_params dp = fs_params_default();
+  if (!params) params = &dp;
+  int rc = fs_check_params(ctx, params);
+  if (rc) return rc;
+  cudaSetDevice(ctx->device);
+  fs_plan *p = (fs_plan *)calloc(1, sizeof(fs_plan));
+  if (!p) return fs_fail(ctx, FS_ERR_NOMEM, "calloc(plan)");
+  p->ctx = ctx;
+  p->nviews = nviews;
+  p->nmaps = nmaps;
+  p->params = *params;
+  p->hf = params->height_filter == FS_BILINEAR;
+  p->cf = params->color_filter == FS_BILINEAR;
+  for (int i = 0; i < nmaps; i++) p->maps[i] = maps[i]->dev;
+  p->views_h = (fs_view *)malloc(sizeof(fs_view) * (size_t)nviews);
+  p->fv_h = (FsView *)malloc(sizeof(FsView) * (size_t)nviews);
+  p->ncap = (int32_t *)malloc(sizeof(int32_t) * (size_t)nviews);
+  p->offsets = (int64_t *)malloc(sizeof(int64_t) * (size_t)nviews);
+  p->tm_h = (CUtensorMap *)aligned_alloc(128, sizeof(CUtensorMap) * (size_t)nviews);
+  if (!p->views_h || !p->fv_h || !p->ncap || !p->offsets || !p->tm_h) {
+    fs_plan_free(p);
+    return fs_fail(ctx, FS_ERR_NOMEM, "malloc(plan arrays)");
+  }
+  memcpy(p->views_h, views, sizeof(fs_view) * (size_t)nviews);
+  int64_t zoff = 0, px = 0;
+  int32_t hmax = 1;
+  for (int v = 0; v < nviews; v++) {
+    const fs_view *vw = &views[v];
+    if (vw->map < 0 || vw->map >= nmaps) {
+      fs_plan_free(p);
+      return fs_fail(ctx, FS_ERR_ARG, "view %d: map index %d out of range", v, vw->map);
+    }
+    rc = fs_make_view(ctx, &vw->cam, params, vw->width, vw->height, vw->map, &p->fv_h[v]);
+    if (rc) {
+      fs_plan_free(p);
+      return rc;
+    }
+    p->fv_h[v].zoff = zoff;
+    p->ncap[v] = p->fv_h[v].n;
+    zoff += p->fv_h[v].n;
+    p->offsets[v] = px;
+    px += ((int64_t)vw->width * vw->height + 63) & ~(int64_t)63; /* 256-byte aligned frames */
+    if (vw->height > hmax) hmax = vw->height;
+  }
+  p->ztotal = zoff;
+  p->total_px = px;
+  p->stride_max = hmax | 1;
+  int e = cudaMalloc((void **)&p->fv_d, sizeof(FsView) * (size_t)nviews);
+  if (!e) e = cudaMalloc((void **)&p->head_d, sizeof(int32_t));
+  if (!e) e = cudaMalloc((void **)&p->zline, sizeof(float4) * (size_t)zoff);
+  if (!e) e = cudaMalloc((void **)&p->zinvz, sizeof(float) * (size_t)zoff);
+  if (!e) e = cudaMalloc((void **)&p->frames, sizeof(uint32_t) * (size_t)px);
+  if (!e && ctx->use_tma) e = cudaMalloc((void **)&p->tm_d, sizeof(CUtensorMap) * (size_t)nviews);
+  if (e) {
+    fs_plan_free(p);
+    return fs_fail(ctx, FS_ERR_NOMEM, "cudaMalloc(plan: %lld frame pixels)", (long long)px);
+  }
+  /* tuning: cache entry for this batch signature, else the default */
+  char key[96];
+  snprintf(key, sizeof(key), "batch:%016llx:map%dx%d:f%d", (unsigned long long)batch_signature(p),
+           p->maps[0].MH, p->maps[0].MW, p->hf | (p->cf << 1));
+  FsTune t;
+  if (!fs_tune_lookup_key(ctx, key, &t) || !fs_tune_fits(ctx, &t, p->stride_max))
+    t = fs_default_batch_tune(ctx, p->stride_max);
+  if (!t.tw) {
+    fs_plan_free(p);
+    return fs_fail(ctx, FS_ERR_ARG, "no kernel configuration fits screen height %d", hmax);
+  }
+  p->tune = t;
+  rc = plan_build(p);
+  if (rc) {
+    fs_plan_free(p);
+    return rc;
+  }
+  *out = p;
+  return FS_OK;
+}
+
+int fs_plan_set_cameras(fs_plan *p, const fs_camera *cams, int32_t ncams) {
+  if (!p || !cams) return FS_ERR_ARG;
+  fs_ctx *ctx = p->ctx;
+  if (ncams != p->nviews) return fs_fail(ctx, FS_ERR_ARG, "expected %d cameras", p->nviews);
+  for (int v = 0; v < p->nviews; v++) {
+    FsView nv;
+    const fs_view *vw = &p->views_h[v];
+    int rc = fs_make_view(ctx, &cams[v], &p->params, vw->width, vw->height, vw->map, &nv);
+    if (rc) return rc;
+    if (nv.n > p->ncap[v])
+      return fs_fail(ctx, FS_ERR_ARG, "view %d: %d depth samples exceed the plan's %d", v, nv.n,
+                     p->ncap[v]);
+    nv.zoff = p->fv_h[v].zoff;
+    nv.out = p->fv_h[v].out;
+    nv.tmap = p->fv_h[v].tmap;
+    p->fv_h[v] = nv;
+    p->views_h[v].cam = cams[v];
+  }
+  cudaSetDevice(ctx->device);
+  int e = cudaMemcpyAsync(p->fv_d, p->fv_h, sizeof(FsView) * (size_t)p->nviews,
+                          cudaMemcpyHostToDevice, ctx->stream);
+  if (e) return fs_cuda_fail(ctx, e, "camera upload");
+  return FS_OK;
+}
+
+int fs_plan_run(fs_plan *p) {
+  if (!p) return FS_ERR_ARG;
+  fs_ctx *ctx = p->ctx;
+  if (!p->graph_ok) return fs_fail(ctx, FS_ERR_STATE, "plan has no graph");
+  cudaSetDevice(ctx->device);
+  int e = cudaGraphLaunch(p->exec, ctx->stream);
+  if (e) return fs_cuda_fail(ctx, e, "cudaGraphLaunch");
+  ctx->launches += 2;
+  return FS_OK;
+}
+
+int fs_plan_run_per_view(fs_plan *p) {
+  if (!p) return FS_ERR_ARG;
+  fs_ctx *ctx = p->ctx;
+  cudaSetDevice(ctx->device);
+  for (int v = 0; v < p->nviews; v++) {
+    FsView fv = p->fv_h[v];
+    FsTune t;
+    if (!fs_tune_lookup(ctx, fv.W, fv.H, p->maps[fv.map].MH, p->maps[fv.map].MW, fv.flags, &t) ||
+        !fs_tune_fits(ctx, &t, fv.H | 1))
+      t = fs_default_tune(ctx, fv.H | 1);
+    CUtensorMap tm __attribute__((aligned(128)));
+    const int have_tm = fs_encode_frame_map(ctx, fv.out, fv.W, fv.H, t.tw, &tm);
+    int rc = fs_render_view(ctx, &p->maps[fv.map], &fv, &t, p->zline, p->zinvz,
+                            have_tm ? &tm : NULL);
+    if (rc) return rc;
+  }
+  return FS_OK;
+}
+
+uint32_t *fs_plan_frame_dev(fs_plan *p, int32_t view) {
+  if (!p || view < 0 || view >= p->nviews) return NULL;
+  return p->frames + p->offsets[view];
+}
+
+int64_t fs_plan_frame_offset(const fs_plan *p, int32_t view) {
+  if (!p || view < 0 || view >= p->nviews) return -1;
+  return p->offsets[view];
+}
+
+int64_t fs_plan_total_pixels(const fs_plan *p) { return p ? p->total_px : 0; }
+
+int fs_plan_download(fs_plan *p, uint32_t *host) {
+  if (!p || !host) return FS_ERR_ARG;
+  fs_ctx *ctx = p->ctx;
+  cudaSetDevice(ctx->device);
+  int e = cudaMemcpyAsync(host, p->frames, sizeof(uint32_t) * (size_t)p->total_px,
+                          cudaMemcpyDeviceToHost, ctx->stream);
+  if (!e) e = cudaStreamSynchronize(ctx->stream);
+  if (e) return fs_cuda_fail(ctx, e, "frame download");
+  return FS_OK;
+}
+
+int fs_plan_get_tune(const fs_plan *p, int32_t out5[5]) {
+  if (!p || !out5) return FS_ERR_ARG;
+  out5[0] = p->tune.tw;
+  out5[1] = p->tune.lc;
+  out5[2] = p->tune.u;
+  out5[3] = p->tune.stage;
+  out5[4] = p->grid;
+  return FS_OK;
+}
+
+int fs_plan_set_tune(fs_plan *p, const int32_t tune5[5]) {
+  if (!p || !tune5) return FS_ERR_ARG;
+  FsTune t = {tune5[0], tune5[1], tune5[2], tune5[3], tune5[4]};
+  if (!fs_tune_fits(p->ctx, &t, p->stride_max))
+    return fs_fail(p->ctx, FS_ERR_ARG, "tuning (%d,%d,%d,%d) unsupported or too large", t.tw,
+                   t.lc, t.u, t.stage);
+  p->tune = t;
+  return plan_build(p);
+}

@@ -1,0 +1,108 @@
+/* Private host-side definitions of the C library (not part of the ABI). */
+#ifndef FS_PRIV_H
+#define FS_PRIV_H
+
+#include <stdint.h>
+
+#include "fs_internal.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FS_TUNE_CACHE_MAX 256
+
+typedef struct {
+  char key[96];
+  FsTune tune;
+} fs_tune_entry;
+
+struct fs_ctx {
+  int32_t device;
+  int32_t broken;
+  cudaStream_t own_stream;
+  cudaStream_t stream;
+  char err[1024];
+  int32_t has_err;
+  void *encode; /* cuTensorMapEncodeTiled, NULL when the driver lacks it */
+  int32_t use_tma;
+  int32_t sm_count;
+  size_t smem_optin;
+  float4 *zline; /* single-frame depth table */
+  float *zinvz;
+  int64_t zcap;
+  uint32_t *frame_dev; /* device frame for fs_render with host output */
+  size_t frame_cap;
+  unsigned long long *stats_dev;
+  int32_t collect_stats;
+  int64_t launches;
+  FsTune forced; /* tw == 0: choose per frame */
+  int32_t ntune;
+  fs_tune_entry tunes[FS_TUNE_CACHE_MAX];
+  char tune_path[512];
+};
+
+struct fs_map {
+  FsMapDev dev;
+  int32_t owned; /* 1: quads and colours owned; 2: quads owned, colours borrowed */
+  uint32_t *q;
+  uint32_t *c;
+  int64_t rows, cols;
+};
+
+struct fs_plan {
+  fs_ctx *ctx;
+  int32_t nviews, nmaps;
+  fs_params params;
+  fs_view *views_h;
+  FsView *fv_h;        /* host copy of the kernel view records */
+  int32_t *ncap;       /* depth capacity per view (n at plan creation) */
+  FsView *fv_d;
+  CUtensorMap *tm_h;   /* 128-byte aligned host array */
+  CUtensorMap *tm_d;
+  int32_t *items_d;
+  int32_t nitems;
+  int32_t *head_d;
+  float4 *zline;
+  float *zinvz;
+  int64_t ztotal;
+  uint32_t *frames;
+  int64_t *offsets;
+  int64_t total_px;
+  FsMapDev maps[FS_MAX_MAPS];
+  FsTune tune;
+  int32_t grid;
+  int32_t stride_max;
+  int32_t hf, cf;
+  cudaGraph_t graph;
+  cudaGraphExec_t exec;
+  int32_t graph_ok;
+};
+
+int fs_fail(fs_ctx *ctx, int code, const char *fmt, ...);
+int fs_cuda_fail(fs_ctx *ctx, int e, const char *what);
+int32_t fs_f2i_host(float v);
+int fs_check_params(fs_ctx *ctx, const fs_params *p);
+int fs_make_view(fs_ctx *ctx, const fs_camera *cam, const fs_params *p, int32_t W, int32_t H,
+                 int32_t map, FsView *v);
+int fs_ensure_ztable(fs_ctx *ctx, int64_t n);
+int fs_encode_frame_map(fs_ctx *ctx, uint32_t *frame, int32_t W, int32_t H, int32_t tw,
+                        CUtensorMap *out);
+int fs_render_view(fs_ctx *ctx, const FsMapDev *map, FsView *v, const FsTune *tune,
+                   float4 *zline, float *zinvz, const CUtensorMap *tmap_pre);
+int fs_tune_fits(fs_ctx *ctx, const FsTune *t, int32_t stride_max);
+FsTune fs_default_tune(fs_ctx *ctx, int32_t stride_max);
+int fs_tune_count(void);
+int fs_tune_get(int i, int32_t out5[5]);
+
+/* tuning cache (fs_tune.c) */
+void fs_tune_cache_load(fs_ctx *ctx);
+int fs_tune_lookup(fs_ctx *ctx, int32_t W, int32_t H, int32_t MH, int32_t MW, int32_t flags,
+                   FsTune *out);
+int fs_tune_lookup_key(fs_ctx *ctx, const char *key, FsTune *out);
+FsTune fs_default_batch_tune(fs_ctx *ctx, int32_t stride_max);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,347 @@
+/*
+ * The voxel-space column renderer (fut/voxel_renderer.fut:214-251, `#off`).
+ *
+ * Work item = (view, column tile of TW screen columns). One CTA renders an
+ * item; with a work counter the CTAs are persistent and pull items until the
+ * queue is empty, so views of uneven size and depth share one launch.
+ *
+ * Lanes: each screen column is marched by LC lanes of a warp (32/LC columns
+ * per warp). A chunk covers LC*U consecutive depths; at step u the LC lanes of
+ * a column take depths k0 + u*LC + 0..LC-1, so every gather instruction covers
+ * a compact patch of the map (LC consecutive depths x 32/LC neighbouring
+ * columns). For each sample the lanes gather the height quad, project the
+ * height to a screen row in f32 and clamp it to [0, H].
+ *
+ * Occlusion: the reference's inclusive `occlude` scan keeps the nearer sample
+ * on ties (:69-72), the scatter writes a colour at every new minimum row (:244)
+ * and the forward fill (:246) paints each row with the nearest sample whose row
+ * lies at or above it. So a sample is an EVENT iff its row is strictly below the
+ * running minimum row of its column, and it paints rows [row, previous minimum).
+ * A segmented warp scan (__shfl_up_sync) over the LC lanes gives each sample the
+ * running minimum before it. Rows >= H are never events, and once the minimum
+ * reaches row 0 no later sample can be one, so the column stops early without
+ * changing a pixel.
+ *
+ * Colours are needed only for events: they go to a warp-private ring in shared
+ * memory and are coloured 32 at a time (all lanes busy). Painting then takes one
+ * of two forms (template STG):
+ *  STG = 1: into a column stage in shared memory (column-major, odd stride: no
+ *           bank conflicts when painting a column or reading a row across
+ *           columns); after the march each column gets the reference's gap fill
+ *           and sky, and the tile is transposed through a row-major box buffer
+ *           and written with TMA bulk tensor stores (cp.async.bulk.tensor.2d),
+ *           32 rows per box, double buffered.
+ *  STG = 0: straight into the frame in global memory (tiny shared-memory
+ *           footprint, full occupancy); sky rows are written row-wise by the
+ *           CTA afterwards, and a column that painted a gap colour gets the gap
+ *           fill re-run over its rows.
+ */
+#pragma once
+#include "fs_device.cuh"
+
+namespace fsd {
+
+template <int U>
+struct QueueCap {
+  static constexpr int raw = 31 + 32 * U;
+  static constexpr int value = raw <= 64 ? 64 : (raw <= 128 ? 128 : (raw <= 256 ? 256 : 512));
+};
+
+constexpr int kBoxRows = 32;
+
+/* Queue entry: depth index (20 bits) | tile column (6) | row (16) | prev (16). */
+__device__ __forceinline__ unsigned long long pack_event(int k, int col, int row, int prev) {
+  return ((unsigned long long)(uint32_t)k << 38) | ((unsigned long long)(uint32_t)col << 32) |
+         ((unsigned long long)(uint32_t)row << 16) | (unsigned long long)(uint32_t)prev;
+}
+
+__device__ __forceinline__ void fence_proxy_async_shared() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap *tm, const void *src, int x, int y) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(src);
+  asm volatile(
+      "cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%2, %3}], [%1];" ::"l"(
+          (unsigned long long)tm),
+      "r"(s), "r"(x), "r"(y)
+      : "memory");
+}
+__device__ __forceinline__ void bulk_commit() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+template <int N>
+__device__ __forceinline__ void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void bulk_wait_all() {
+  asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+}
+
+/* fill_vline scan + sky (fut/voxel_renderer.fut:78-81, 246-248) over rows
+ * [y_begin, H) of one column, one warp, 32 rows per step. `at(y)` addresses row
+ * y. Rows above the column's final minimum row `mf` were never painted and
+ * hold the gap value. */
+template <class At>
+__device__ __forceinline__ void fill_column(At at, int y_begin, int H, int mf, uint32_t gap,
+                                            uint32_t sky, int lane) {
+  unsigned lemask;
+  asm("mov.u32 %0, %%lanemask_le;" : "=r"(lemask));
+  uint32_t carry = gap;
+  for (int y0 = y_begin; y0 < H; y0 += 32) {
+    const int y = y0 + lane;
+    uint32_t v = gap;
+    if (y < H && y >= mf) v = *at(y);
+    const unsigned nz = __ballot_sync(FS_FULL_MASK, v != gap);
+    const unsigned le = nz & lemask;
+    const int src = le ? 31 - __clz(le) : 0;
+    const uint32_t t = __shfl_sync(FS_FULL_MASK, v, src);
+    const uint32_t val = le ? t : carry;
+    if (y < H) *at(y) = (val == gap) ? sky : val;
+    if (nz) carry = __shfl_sync(FS_FULL_MASK, v, 31 - __clz(nz));
+  }
+}
+
+template <int TW, int LC, int U, int STG>
+struct RenderShape {
+  static constexpr int NT = TW * LC;
+  static constexpr int NW = NT / 32;
+  static constexpr int CPW = 32 / LC;
+  static constexpr int QCAP = QueueCap<U>::value;
+  static constexpr size_t box_bytes = STG ? 2ull * kBoxRows * TW * 4 : 0;
+  static constexpr size_t queue_bytes = (size_t)NW * QCAP * 8;
+  static constexpr size_t lut_bytes = 256 * 4;
+  static constexpr size_t meta_bytes = (size_t)TW * 8;
+  static constexpr size_t fixed_bytes = box_bytes + queue_bytes + lut_bytes + meta_bytes;
+  static constexpr int min_blocks = STG ? 1 : (NT >= 1024 ? 1 : 1024 / NT);
+};
+
+template <int TW, int LC, int U, int HF, int CF, int STG>
+__global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG>::min_blocks))
+    render_kernel(const __grid_constant__ FsLaunch P) {
+  using S = RenderShape<TW, LC, U, STG>;
+  constexpr int NT = S::NT;
+  constexpr int CPW = S::CPW;
+  constexpr int CH = LC * U;
+  constexpr int QCAP = S::QCAP;
+  static_assert(NT % 32 == 0 && 32 % LC == 0 && TW % 4 == 0 && TW <= 64, "shape");
+
+  extern __shared__ __align__(1024) unsigned char smem[];
+  uint32_t *box = reinterpret_cast<uint32_t *>(smem);
+  unsigned long long *queues = reinterpret_cast<unsigned long long *>(smem + S::box_bytes);
+  float *lut = reinterpret_cast<float *>(smem + S::box_bytes + S::queue_bytes);
+  int *col_mf = reinterpret_cast<int *>(smem + S::box_bytes + S::queue_bytes + S::lut_bytes);
+  int *col_flag = col_mf + TW;
+  uint32_t *stage = reinterpret_cast<uint32_t *>(smem + S::fixed_bytes);
+  __shared__ int s_item;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int dl = lane % LC;
+  const int cl = warp * CPW + lane / LC;
+  unsigned long long *q = queues + warp * QCAP;
+  unsigned lanemask_lt;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lanemask_lt));
+  for (int i = tid; i < 256; i += NT) lut[i] = __fdiv_rn((float)i, 255.0f);
+  const Channels chan{lut};
+  unsigned long long n_samples = 0, n_events = 0;
+
+  for (int iter = 0;; iter++) {
+    int item;
+    if (P.head) {
+      if (tid == 0) s_item = atomicAdd(P.head, 1);
+      if (!STG && tid < TW) col_flag[tid] = 0;
+      __syncthreads();
+      item = s_item;
+    } else {
+      if (!STG && tid < TW) col_flag[tid] = 0;
+      __syncthreads();
+      item = iter == 0 ? (int)blockIdx.x : P.nitems;
+    }
+    if (item >= P.nitems) break;
+    int vi = 0, tile = item;
+    if (P.items) {
+      const int it = P.items[item];
+      vi = it >> 12;
+      tile = it & 4095;
+    }
+    const FsView *Vp = P.views ? P.views + vi : &P.view0;
+    const float cam_h = Vp->cam_h, horizon = Vp->horizon;
+    const int W = Vp->W, H = Vp->H, n = Vp->n;
+    const uint32_t sky = Vp->sky, gap = Vp->gap;
+    const FsMapDev M = P.maps[Vp->map];
+    const float4 *zl = P.zline + Vp->zoff;
+    const float *zi = P.zinvz + Vp->zoff;
+    uint32_t *const out = Vp->out;
+    const int stride = H | 1;
+    const int c0 = tile * TW;
+    const int col = c0 + cl;
+    const bool valid = col < W;
+    const float fcol = (float)col;
+
+    int m = H;          /* running minimum row of this column */
+    int qh = 0, qt = 0; /* ring head / tail, warp-uniform */
+
+    /* colour the queued events [qh, qh+cnt) and paint their intervals */
+    auto drain = [&](int cnt) {
+      if (lane < cnt) {
+        const unsigned long long e = q[(qh + lane) & (QCAP - 1)];
+        const int k = (int)(e >> 38);
+        const int ecl = (int)((e >> 32) & 63u);
+        const int er = (int)((e >> 16) & 0xFFFFu);
+        const int ep = (int)(e & 0xFFFFu);
+        const float ec = (float)(c0 + ecl);
+        const float4 L = __ldg(zl + k);
+        const float x = fa(L.x, fm(ec, L.z));
+        const float y = fa(L.y, fm(ec, L.w));
+        const uint32_t colour = CF ? color_bilinear(M, chan, x, y) : color_nearest(M, x, y);
+        if (STG) {
+          uint32_t *sc = stage + ecl * stride;
+          for (int yy = er; yy < ep; yy++) sc[yy] = colour;
+        } else {
+          uint32_t *o = out + (size_t)er * W + c0 + ecl;
+          for (int yy = er; yy < ep; yy++, o += W) *o = colour;
+          if (colour == gap) col_flag[ecl] = 1;
+        }
+      }
+      __syncwarp();
+    };
+
+    for (int k0 = 0; k0 < n; k0 += CH) {
+      if (__all_sync(FS_FULL_MASK, !valid || m == 0)) break;
+      int r[U];
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int k = k0 + u * LC + dl;
+        int rr = H;
+        if (valid && m > 0 && k < n) {
+          const float4 L = __ldg(zl + k);
+          const float x = fa(L.x, fm(fcol, L.z));
+          const float y = fa(L.y, fm(fcol, L.w));
+          const float hh = HF ? height_bilinear(M, x, y) : height_nearest(M, x, y);
+          const float rel = fa(fm(fs(cam_h, hh), __ldg(zi + k)), horizon);
+          rr = min(max(f2i(rel), 0), H);
+          n_samples++;
+        }
+        r[u] = rr;
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        int incl = r[u];
+#pragma unroll
+        for (int off = 1; off < LC; off <<= 1) {
+          const int t = __shfl_up_sync(FS_FULL_MASK, incl, off, LC);
+          if (dl >= off) incl = min(incl, t);
+        }
+        const int excl = __shfl_up_sync(FS_FULL_MASK, incl, 1, LC);
+        const int prev = (dl == 0) ? m : min(m, excl);
+        const bool ev = r[u] < prev;
+        const unsigned msk = __ballot_sync(FS_FULL_MASK, ev);
+        if (ev) {
+          const int pos = (qt + __popc(msk & lanemask_lt)) & (QCAP - 1);
+          q[pos] = pack_event(k0 + u * LC + dl, cl, r[u], prev);
+        }
+        qt += __popc(msk);
+        m = min(m, __shfl_sync(FS_FULL_MASK, incl, LC - 1, LC));
+      }
+      __syncwarp();
+      while (qt - qh >= 32) {
+        drain(32);
+        qh += 32;
+      }
+    }
+    if (qt > qh) drain(qt - qh);
+    n_events += (unsigned long long)qt;
+
+    if (STG) {
+      /* gap fill + sky for this warp's columns, then the transposed store */
+#pragma unroll 1
+      for (int c = 0; c < CPW; c++) {
+        const int mf = __shfl_sync(FS_FULL_MASK, m, c * LC);
+        const int lcl = warp * CPW + c;
+        uint32_t *sc = stage + lcl * stride;
+        if (c0 + lcl < W)
+          fill_column([sc](int y) { return sc + y; }, 0, H, mf, gap, sky, lane);
+      }
+      __syncthreads();
+      if (Vp->tmap >= 0) {
+        const CUtensorMap *tm = P.views ? P.tmaps + Vp->tmap : &P.tmap0;
+        const int nb = (H + kBoxRows - 1) / kBoxRows;
+        for (int b = 0; b < nb; b++) {
+          uint32_t *buf = box + (b & 1) * kBoxRows * TW;
+          if (b >= 2) {
+            if (tid == 0) bulk_wait_read<1>();
+            __syncthreads();
+          }
+          for (int e = tid; e < kBoxRows * TW; e += NT) {
+            const int rr = e / TW, cc = e - rr * TW;
+            const int y = b * kBoxRows + rr;
+            buf[e] = (y < H) ? stage[cc * stride + y] : 0u;
+          }
+          fence_proxy_async_shared();
+          __syncthreads();
+          if (tid == 0) {
+            tma_store_2d(tm, buf, c0, b * kBoxRows);
+            bulk_commit();
+          }
+        }
+        if (tid == 0) bulk_wait_read<0>();
+      } else {
+        for (int e = tid; e < H * TW; e += NT) {
+          const int y = e / TW, cc = e - y * TW;
+          if (c0 + cc < W) out[(size_t)y * W + c0 + cc] = stage[cc * stride + y];
+        }
+      }
+    } else {
+      /* final minimum rows, gap re-fill of flagged columns, sky rows */
+      if (dl == 0) col_mf[cl] = m;
+      __syncthreads();
+#pragma unroll 1
+      for (int c = 0; c < CPW; c++) {
+        const int lcl = warp * CPW + c;
+        if (c0 + lcl < W && col_flag[lcl]) {
+          uint32_t *oc = out + c0 + lcl;
+          const int mf = col_mf[lcl];
+          fill_column([oc, W](int y) { return oc + (size_t)y * W; }, mf, H, mf, gap, sky, lane);
+        }
+      }
+      int top = 0;
+      for (int c = 0; c < TW; c++) top = max(top, col_mf[c]);
+      for (int e = tid; e < top * TW; e += NT) {
+        const int y = e / TW, cc = e - y * TW;
+        if (c0 + cc < W && y < col_mf[cc]) out[(size_t)y * W + c0 + cc] = sky;
+      }
+    }
+    __syncthreads();
+  }
+  if (STG && tid == 0) bulk_wait_all();
+  if (P.stats) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+      n_samples += __shfl_down_sync(FS_FULL_MASK, n_samples, off);
+    if (lane == 0) {
+      atomicAdd(reinterpret_cast<unsigned long long *>(P.stats), n_samples);
+      atomicAdd(reinterpret_cast<unsigned long long *>(P.stats) + 1, n_events);
+    }
+  }
+}
+
+}  // namespace fsd
+
+/* The tuning table: (TW, LC, U, STG) compiled for every filter pair. */
+#define FS_TUNE_LIST(X) \
+  X(4, 32, 2, 1)        \
+  X(8, 32, 1, 1)        \
+  X(8, 32, 2, 1)        \
+  X(16, 32, 2, 1)       \
+  X(32, 32, 1, 1)       \
+  X(16, 16, 2, 1)       \
+  X(32, 16, 2, 1)       \
+  X(16, 8, 4, 1)        \
+  X(32, 8, 4, 1)        \
+  X(8, 32, 2, 0)        \
+  X(16, 16, 2, 0)       \
+  X(32, 8, 2, 0)        \
+  X(32, 8, 4, 0)        \
+  X(32, 4, 4, 0)        \
+  X(64, 4, 4, 0)        \
+  X(32, 4, 8, 0)

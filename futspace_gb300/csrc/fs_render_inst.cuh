@@ -1,0 +1,34 @@
+/*
+ * Instantiates the render kernel for one (height filter, colour filter) pair
+ * and every tuning triple of FS_TUNE_LIST. Included by fs_render_h?c?.cu with
+ * FS_HF, FS_CF and FS_RENDER_ENTRY defined, so the four pairs compile as
+ * separate translation units in parallel.
+ *
+ * op 0: launch `grid` CTAs; op 1: occupancy query (CTAs per SM) into *occ.
+ */
+#include "fs_render.cuh"
+
+extern "C" int FS_RENDER_ENTRY(int op, const FsLaunch *L, const FsTune *t, int grid,
+                               size_t smem, cudaStream_t st, int *occ) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return (int)e;
+  if (dev < 0 || dev >= 64) return (int)cudaErrorInvalidDevice;
+#define FS_CASE(TW_, LC_, U_, STG_)                                                        \
+  if (t->tw == TW_ && t->lc == LC_ && t->u == U_ && t->stage == STG_) {                    \
+    static int smem_set[64];                                                               \
+    auto kern = fsd::render_kernel<TW_, LC_, U_, FS_HF, FS_CF, STG_>;                      \
+    if (smem_set[dev] < (int)smem) {                                                       \
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+      if (e != cudaSuccess) return (int)e;                                                 \
+      smem_set[dev] = (int)smem;                                                           \
+    }                                                                                      \
+    if (op == 1) return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern,      \
+                                                                           TW_ * LC_, smem); \
+    kern<<<grid, TW_ * LC_, smem, st>>>(*L);                                               \
+    return (int)cudaGetLastError();                                                        \
+  }
+  FS_TUNE_LIST(FS_CASE)
+#undef FS_CASE
+  return (int)cudaErrorInvalidValue;
+}

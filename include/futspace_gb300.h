@@ -1,0 +1,211 @@
+/*
+ * futspace_gb300: Voxel Space terrain renderer for one NVIDIA GB300 (sm_103a).
+ *
+ * Direct C ABI. Plain pointers and sizes; every function returns an int status
+ * (FS_OK == 0) and never exits the process. The Futhark-compatible names that
+ * the reference's host program links against are in libfutspace.h.
+ *
+ * The renderer is the reference's per-frame `render`
+ * (fut/voxel_renderer.fut:101-251, `#off` branch) with the samplers of
+ * fut/render_functions.fut:63-105, reached from fut/interactive.fut:173-183.
+ */
+#ifndef FUTSPACE_GB300_H
+#define FUTSPACE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define FS_OK 0
+#define FS_ERR_ARG 1      /* bad argument (null pointer, size out of range, ...) */
+#define FS_ERR_CUDA 2     /* a CUDA runtime call failed (text in fs_ctx_get_error) */
+#define FS_ERR_RANGE 3    /* depth schedule has no samples: the reference raises an
+                             invalid-range error on `1...n` (fut/voxel_renderer.fut:33) */
+#define FS_ERR_NOMEM 4    /* host or device allocation failed */
+#define FS_ERR_BUDGET 5   /* serving: request exceeds the framebuffer budget */
+#define FS_ERR_STATE 6    /* object used in the wrong state */
+
+/* ---- value types ---------------------------------------------------------- */
+
+/* Camera record of fut/voxel_renderer.fut:5-12. `horizon` is the screen row of
+ * the horizon (the reference's pitch control, fut/interactive.fut:102-104);
+ * `angle` is the yaw in radians; `distance` the draw distance. */
+typedef struct {
+  float x, y, height, angle, horizon, distance, fov;
+  uint32_t sky_color; /* ARGB */
+} fs_camera;
+
+enum { FS_NEAREST = 0, FS_BILINEAR = 1 };
+enum { FS_GAP_ZERO = 0, FS_GAP_SKY = 1 };
+
+/* Render parameters.
+ *  invz_param1 : depth step d of the arithmetic depth series
+ *                (reference default 0.001, fut/voxel_renderer.fut:104)
+ *  invz_param2 : first depth z0 (default 0.0, :103)
+ *  magic_number: projection scale in inv_z = (1/z) * scale; <= 0 selects the
+ *                reference's f32(w/2) with integer division (:217)
+ *  height_filter, color_filter: FS_BILINEAR is png_height_filtered /
+ *                png_color_filtered (fut/render_functions.fut:67-77, 95-105),
+ *                FS_NEAREST is png_height / png_color (:63-64, 91-92).
+ *  gap_rule    : FS_GAP_ZERO fills colour-0 gaps and then paints 0 as sky
+ *                (fut/voxel_renderer.fut:78-81, 246-248); FS_GAP_SKY treats the
+ *                sky colour as the gap (tests/futspace.fut:110-121).
+ *  floor_n     : 1 floors the depth count before the i32 conversion
+ *                (fut/voxel_renderer.fut:32); 0 converts directly
+ *                (tests/futspace.fut:51). Identical for positive counts.
+ * fs_params_default() gives the live reference path: 0.001, 0.0, w/2,
+ * bilinear height and colour, FS_GAP_ZERO, floor_n 1. */
+typedef struct {
+  float invz_param1;
+  float invz_param2;
+  float magic_number;
+  int32_t height_filter;
+  int32_t color_filter;
+  int32_t gap_rule;
+  int32_t floor_n;
+  int32_t reserved;
+} fs_params;
+
+/* One view of a batch: a camera, a screen size and the map it samples. */
+typedef struct {
+  fs_camera cam;
+  int32_t width, height; /* W columns x H rows */
+  int32_t map;           /* index into the maps given to fs_plan_new */
+  int32_t reserved;
+} fs_view;
+
+typedef struct fs_ctx fs_ctx;
+typedef struct fs_map fs_map;
+typedef struct fs_plan fs_plan;
+
+/* ---- context ------------------------------------------------------------- */
+fs_params fs_params_default(void);
+int fs_ctx_new(fs_ctx **out, int32_t device);
+void fs_ctx_free(fs_ctx *ctx);
+/* Last error text as a malloc'd string the caller frees; NULL when none. */
+char *fs_ctx_get_error(fs_ctx *ctx);
+int fs_ctx_sync(fs_ctx *ctx);
+/* Stream used by every asynchronous call of this context (a cudaStream_t);
+ * NULL restores the context's own stream. */
+int fs_ctx_set_stream(fs_ctx *ctx, void *stream);
+void *fs_ctx_get_stream(fs_ctx *ctx);
+/* Number of render kernels this context launched so far. */
+int64_t fs_ctx_kernel_launches(fs_ctx *ctx);
+/* Kernel configurations are int32_t[5]: {tile width (columns per CTA), lanes
+ * per column, depth samples per lane per chunk, stage (1: shared-memory column
+ * stage + TMA row stores, 0: direct painting), persistent CTAs (0: fill GPU)}.
+ * fs_ctx_force_tune fixes the configuration of every following single-frame
+ * render; NULL or tile width 0 restores the tuning-cache / default choice. */
+int fs_ctx_force_tune(fs_ctx *ctx, const int32_t tune5[5]);
+
+/* ---- maps ---------------------------------------------------------------- */
+/* Copies a [rows][cols] u8 height map and ARGB colour map from host memory to
+ * the device. The maps stay resident until fs_map_free. */
+int fs_map_new(fs_ctx *ctx, fs_map **out, const uint8_t *heights, const uint32_t *colors,
+               int64_t rows, int64_t cols);
+/* Same from i32 heights, keeping the low 8 bits as fut/interactive.fut:189
+ * does (`elem & 0xFF`). */
+int fs_map_new_i32(fs_ctx *ctx, fs_map **out, const int32_t *heights, const uint32_t *colors,
+                   int64_t rows, int64_t cols);
+/* Device-resident inputs: the colours are used in place (the caller keeps them
+ * alive); the heights are read once to build the height quads. */
+int fs_map_wrap_device(fs_ctx *ctx, fs_map **out, const uint8_t *heights_dev,
+                       const uint32_t *colors_dev, int64_t rows, int64_t cols);
+int fs_map_free(fs_ctx *ctx, fs_map *map);
+int fs_map_shape(const fs_map *map, int64_t *rows, int64_t *cols);
+/* Device height quads: [rows][cols] u32, bytes 0..3 = heights at (y,x),
+ * (y,x+1), (y+1,x), (y+1,x+1) with wrapped indices. */
+const uint32_t *fs_map_quads_dev(const fs_map *map);
+const uint32_t *fs_map_colors_dev(const fs_map *map);
+
+/* ---- depth schedule ------------------------------------------------------- */
+/* Number of depth samples get_zs yields for draw distance D
+ * (fut/voxel_renderer.fut:28-34). */
+int32_t fs_num_depths(float distance, const fs_params *params);
+
+/* ---- plain per-frame render ---------------------------------------------- */
+/* Renders one [height][width] ARGB frame into device memory `out_dev`
+ * (row-major, pitch = width), asynchronously on the context stream. */
+int fs_render_device(fs_ctx *ctx, const fs_map *map, const fs_camera *cam,
+                     const fs_params *params, int32_t width, int32_t height,
+                     uint32_t *out_dev);
+/* Same into HOST memory `out_host`: renders, copies the frame back and waits. */
+int fs_render(fs_ctx *ctx, const fs_map *map, const fs_camera *cam, const fs_params *params,
+              int32_t width, int32_t height, uint32_t *out_host);
+
+/* ---- batched multi-view render -------------------------------------------
+ * A plan fixes the views' screen sizes and draw distances, owns a device
+ * framebuffer arena with one frame per view, and renders every view with one
+ * persistent kernel that pulls (view, column-tile) items from a device queue.
+ * The launch sequence is captured once into a CUDA graph and replayed. */
+int fs_plan_new(fs_ctx *ctx, fs_plan **out, const fs_map *const *maps, int32_t nmaps,
+                const fs_params *params, const fs_view *views, int32_t nviews);
+void fs_plan_free(fs_plan *plan);
+/* Replaces the cameras (same count; draw distances must not raise any view's
+ * depth count above the one the plan was built with). */
+int fs_plan_set_cameras(fs_plan *plan, const fs_camera *cams, int32_t ncams);
+/* Enqueues one render of every view on the context stream. */
+int fs_plan_run(fs_plan *plan);
+/* Renders with one plain launch pair per view instead (the comparison loop). */
+int fs_plan_run_per_view(fs_plan *plan);
+uint32_t *fs_plan_frame_dev(fs_plan *plan, int32_t view);
+int64_t fs_plan_frame_offset(const fs_plan *plan, int32_t view); /* in pixels */
+int64_t fs_plan_total_pixels(const fs_plan *plan);
+/* Copies every frame to `host` (fs_plan_total_pixels u32 values, frames laid
+ * out at fs_plan_frame_offset) and waits. */
+int fs_plan_download(fs_plan *plan, uint32_t *host);
+/* Kernel configuration the plan uses (see fs_ctx_force_tune); out5[4] is the
+ * persistent grid size actually launched. */
+int fs_plan_get_tune(const fs_plan *plan, int32_t out5[5]);
+int fs_plan_set_tune(fs_plan *plan, const int32_t tune5[5]);
+/* Order-independent hash of the plan's resolution multiset (tuning-cache key). */
+int fs_plan_signature(const fs_plan *plan, int64_t *sig);
+
+/* ---- autotuner -------------------------------------------------------------
+ * Times every compiled (tile width, lanes per column, depth samples per lane)
+ * configuration that fits in shared memory and caches the fastest per
+ * (resolution, map size, filters) -- or per batch resolution multiset -- in the
+ * text file $FS_TUNE_CACHE (default ./.futspace_tune.txt). */
+int fs_autotune_frame(fs_ctx *ctx, const fs_map *map, const fs_camera *cam,
+                      const fs_params *params, int32_t width, int32_t height, int32_t reps,
+                      int32_t out5[5], float *best_ms);
+int fs_plan_autotune(fs_plan *plan, int32_t reps, int32_t out5[5], float *best_ms);
+/* Number of compiled configurations and the i-th one as {tw, lc, u, stage, 0}. */
+int fs_tune_count(void);
+int fs_tune_get(int i, int32_t out5[5]);
+
+/* Work counters of the render kernel: when enabled, every following launch adds
+ * the depth samples it evaluated and the occlusion events it coloured. Reading
+ * (out2 != NULL) waits for the stream and resets the counters. */
+int fs_ctx_stats(fs_ctx *ctx, int32_t enable, uint64_t out2[2]);
+
+/* ---- synthetic inputs (seeded, identical on every host) -------------------- */
+/* Toroidal diamond-square height map, rescaled to 0..255. size must be a power
+ * of two. */
+int fsgen_heights(uint64_t seed, int32_t size, float roughness, uint8_t *out);
+/* 5-stop terrain palette indexed by height, plus uniform +-noise per channel,
+ * alpha 0xFF. */
+int fsgen_colors(uint64_t seed, const uint8_t *heights, int64_t count, int32_t noise,
+                 uint32_t *out);
+/* Maximum height in the 16x16 window centred on (x, y), wrapping. */
+int32_t fsgen_local_max(const uint8_t *heights, int32_t rows, int32_t cols, float x, float y);
+/* `count` cameras uniform on the map: yaw uniform in [0, 2pi), height in
+ * [lo, hi] above the local maximum, horizon = screen_h / 2, fov 1.2. */
+int fsgen_cameras(uint64_t seed, const uint8_t *heights, int32_t rows, int32_t cols,
+                  int32_t count, float above_lo, float above_hi, float distance_lo,
+                  float distance_hi, int32_t screen_h, fs_camera *out);
+/* A random walk of `count` frames: each frame turns by U(-yaw, yaw), moves
+ * `step` map units forward and keeps the height within [lo, hi] above the
+ * local maximum. */
+int fsgen_walk(uint64_t seed, const uint8_t *heights, int32_t rows, int32_t cols,
+               int32_t count, float step, float yaw, float above_lo, float above_hi,
+               float distance, int32_t screen_h, fs_camera *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
