@@ -214,6 +214,9 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batch512", choices=["batch512", "walk1080"])
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--tune", default="",
+                    help="pin the plan's kernel configuration: tile_width,lanes_per_column,"
+                         "depth_per_lane,stage (skips the autotuner)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
@@ -243,7 +246,9 @@ def main():
     fmap = fs.Map(ctx, hm, cm)
     plan = fs.Plan(ctx, [fmap], views)
     tune_info = None
-    if not args.no_autotune:
+    if args.tune:
+        plan.set_tune(*[int(x) for x in args.tune.split(",")])
+    elif not args.no_autotune:
         tune_info = plan.autotune(reps=3)
     tune = plan.get_tune()
     px = sum(w * h for _, w, h in views)
@@ -291,6 +296,12 @@ def main():
 
     t_plain = []
     if not args.no_plain:
+        # the per-frame loop runs each resolution with its own autotuned configuration
+        seen = set()
+        for cam, w, h in views:
+            if (w, h) not in seen:
+                seen.add((w, h))
+                ctx.autotune_frame(fmap, cam, w, h, reps=3)
         plan.run_per_view()
         ctx.sync()
         t_plain = timed(plan.run_per_view, max(3, args.steps // 2))

@@ -11,7 +11,10 @@ fut/render_functions.fut:63-105.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
+import sys
+import weakref
 from pathlib import Path
 from typing import Iterable, Sequence
 
@@ -62,6 +65,28 @@ def library_path() -> Path:
 
 
 _LIB = None
+# Live native objects, released in dependency order (plans, maps, contexts) at
+# interpreter exit, while the CUDA runtime is still up; __del__ does nothing
+# during finalisation.
+_LIVE: "weakref.WeakSet" = weakref.WeakSet()
+
+
+def _release_all():
+    objs = list(_LIVE)
+    for kind in (Plan, Map, Context):
+        for o in objs:
+            if isinstance(o, kind):
+                try:
+                    o.close()
+                except Exception:
+                    pass
+
+
+atexit.register(_release_all)
+
+
+def _finalizing() -> bool:
+    return sys.is_finalizing()
 
 
 def _sig(lib, name, res, args):
@@ -205,6 +230,7 @@ class Context:
                 lib().fs_ctx_free(self._h)
                 self._h = C.c_void_p()
             raise FsError(rc, msg or "fs_ctx_new")
+        _LIVE.add(self)
 
     @property
     def handle(self):
@@ -259,6 +285,8 @@ class Context:
         self.close()
 
     def __del__(self):
+        if _finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -310,6 +338,7 @@ class Map:
         ctx.check(fn(ctx.handle, C.byref(self._h), _ptr(h), _ptr(c), h.shape[0], h.shape[1]),
                   "fs_map_new")
         self.shape = h.shape
+        _LIVE.add(self)
 
     @property
     def handle(self):
@@ -321,6 +350,8 @@ class Map:
             self._h = C.c_void_p()
 
     def __del__(self):
+        if _finalizing():
+            return
         try:
             self.close()
         except Exception:
@@ -347,6 +378,7 @@ class Plan:
                                     C.byref(self.params), arr, len(views)), "fs_plan_new")
         self.sizes = [(v[1], v[2]) for v in views]
         self.nviews = len(views)
+        _LIVE.add(self)
 
     @property
     def handle(self):
@@ -409,6 +441,8 @@ class Plan:
             self._h = C.c_void_p()
 
     def __del__(self):
+        if _finalizing():
+            return
         try:
             self.close()
         except Exception:

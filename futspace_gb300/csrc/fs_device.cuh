@@ -103,10 +103,10 @@ __device__ __forceinline__ uint32_t mix(const Channels &ch, float w1, uint32_t c
 __device__ __forceinline__ uint32_t color_bilinear(const FsMapDev &M, const Channels &ch,
                                                    float x, float y) {
   const float fx = floorf(x), cx = ceilf(x), fy = floorf(y), cy = ceilf(y);
-  const int32_t ix0 = wrap(f2i(fx), M.MW, M.pow2), ix1 = wrap(f2i(cx), M.MW, M.pow2);
-  const int32_t iy0 = wrap(f2i(fy), M.MH, M.pow2), iy1 = wrap(f2i(cy), M.MH, M.pow2);
-  const uint32_t *r0 = M.c + (size_t)iy0 * (size_t)M.MW;
-  const uint32_t *r1 = M.c + (size_t)iy1 * (size_t)M.MW;
+  const int32_t ix0 = wrap(f2i(fx), M.CW, M.cpow2), ix1 = wrap(f2i(cx), M.CW, M.cpow2);
+  const int32_t iy0 = wrap(f2i(fy), M.CH, M.cpow2), iy1 = wrap(f2i(cy), M.CH, M.cpow2);
+  const uint32_t *r0 = M.c + (size_t)iy0 * (size_t)M.CW;
+  const uint32_t *r1 = M.c + (size_t)iy1 * (size_t)M.CW;
   const uint32_t c00 = __ldg(r0 + ix0), c01 = __ldg(r0 + ix1);
   const uint32_t c10 = __ldg(r1 + ix0), c11 = __ldg(r1 + ix1);
   const uint32_t x1 = mix(ch, fs(cx, x), c00, fs(x, fx), c01);
@@ -116,8 +116,8 @@ __device__ __forceinline__ uint32_t color_bilinear(const FsMapDev &M, const Chan
 
 /* png_color, fut/render_functions.fut:91-92 */
 __device__ __forceinline__ uint32_t color_nearest(const FsMapDev &M, float x, float y) {
-  const int32_t ix = wrap(f2i(x), M.MW, M.pow2), iy = wrap(f2i(y), M.MH, M.pow2);
-  return __ldg(M.c + (size_t)iy * (size_t)M.MW + ix);
+  const int32_t ix = wrap(f2i(x), M.CW, M.cpow2), iy = wrap(f2i(y), M.CH, M.cpow2);
+  return __ldg(M.c + (size_t)iy * (size_t)M.CW + ix);
 }
 
 }  // namespace fsd

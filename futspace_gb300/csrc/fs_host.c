@@ -296,9 +296,9 @@ static int fs_map_alloc(fs_ctx *ctx, fs_map **out, int64_t rows, int64_t cols) {
   m->cols = cols;
   m->dev.q = m->q;
   m->dev.c = m->c;
-  m->dev.MH = (int32_t)rows;
-  m->dev.MW = (int32_t)cols;
-  m->dev.pow2 = is_pow2(rows) && is_pow2(cols);
+  m->dev.MH = m->dev.CH = (int32_t)rows;
+  m->dev.MW = m->dev.CW = (int32_t)cols;
+  m->dev.pow2 = m->dev.cpow2 = is_pow2(rows) && is_pow2(cols);
   *out = m;
   return FS_OK;
 }
@@ -371,9 +371,9 @@ int fs_map_wrap_device(fs_ctx *ctx, fs_map **out, const uint8_t *heights_dev,
   m->cols = cols;
   m->dev.q = m->q;
   m->dev.c = colors_dev;
-  m->dev.MH = (int32_t)rows;
-  m->dev.MW = (int32_t)cols;
-  m->dev.pow2 = is_pow2(rows) && is_pow2(cols);
+  m->dev.MH = m->dev.CH = (int32_t)rows;
+  m->dev.MW = m->dev.CW = (int32_t)cols;
+  m->dev.pow2 = m->dev.cpow2 = is_pow2(rows) && is_pow2(cols);
   int e = fsk_build_quads(heights_dev, m->q, (int32_t)rows, (int32_t)cols, ctx->stream);
   if (!e) e = cudaStreamSynchronize(ctx->stream);
   if (e) {
@@ -412,6 +412,8 @@ static const FsTune k_tune_order[] = {
     {32, 32, 1, 1, 0}, {16, 16, 2, 1, 0}, {32, 16, 2, 1, 0}, {16, 8, 4, 1, 0},
     {32, 8, 4, 1, 0},  {8, 32, 2, 0, 0},  {16, 16, 2, 0, 0}, {32, 8, 2, 0, 0},
     {32, 8, 4, 0, 0},  {32, 4, 4, 0, 0},  {64, 4, 4, 0, 0},  {32, 4, 8, 0, 0},
+    {64, 2, 4, 0, 0},  {64, 1, 4, 0, 0},  {128, 1, 4, 0, 0}, {64, 1, 8, 0, 0},
+    {128, 1, 8, 0, 0},
 };
 
 int fs_tune_count(void) { return (int)(sizeof(k_tune_order) / sizeof(k_tune_order[0])); }

@@ -48,10 +48,12 @@ typedef struct {
  * whole bilinear footprint; byte 0 alone is the nearest sample. */
 typedef struct {
   const uint32_t *q;  /* [MH][MW] height quads */
-  const uint32_t *c;  /* [MH][MW] ARGB colours */
-  int32_t MH, MW;
-  int32_t pow2;       /* both sizes powers of two: wrap with a mask */
-  int32_t pad;
+  const uint32_t *c;  /* [CH][CW] ARGB colours */
+  int32_t MH, MW;     /* height map rows, columns */
+  int32_t CH, CW;     /* colour map rows, columns (the interactive app samples a
+                         1024x1024 shadowed colour map over any height map) */
+  int32_t pow2;       /* MH and MW are powers of two: wrap with a mask */
+  int32_t cpow2;      /* CH and CW are powers of two */
 } FsMapDev;
 
 /* Everything one render launch needs, passed by value (__grid_constant__), so

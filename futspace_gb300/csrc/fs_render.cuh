@@ -49,9 +49,9 @@ struct QueueCap {
 
 constexpr int kBoxRows = 32;
 
-/* Queue entry: depth index (20 bits) | tile column (6) | row (16) | prev (16). */
+/* Queue entry: depth index (20 bits) | tile column (7) | row (16) | prev (16). */
 __device__ __forceinline__ unsigned long long pack_event(int k, int col, int row, int prev) {
-  return ((unsigned long long)(uint32_t)k << 38) | ((unsigned long long)(uint32_t)col << 32) |
+  return ((unsigned long long)(uint32_t)k << 39) | ((unsigned long long)(uint32_t)col << 32) |
          ((unsigned long long)(uint32_t)row << 16) | (unsigned long long)(uint32_t)prev;
 }
 
@@ -113,6 +113,8 @@ struct RenderShape {
   static constexpr size_t lut_bytes = 256 * 4;
   static constexpr size_t meta_bytes = (size_t)TW * 8;
   static constexpr size_t fixed_bytes = box_bytes + queue_bytes + lut_bytes + meta_bytes;
+  /* direct painting keeps 64 registers per thread so 32 warps fit per SM:
+   * the march is bound by gather latency, and occupancy hides it */
   static constexpr int min_blocks = STG ? 1 : (NT >= 1024 ? 1 : 1024 / NT);
 };
 
@@ -124,7 +126,7 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG>::min_bloc
   constexpr int CPW = S::CPW;
   constexpr int CH = LC * U;
   constexpr int QCAP = S::QCAP;
-  static_assert(NT % 32 == 0 && 32 % LC == 0 && TW % 4 == 0 && TW <= 64, "shape");
+  static_assert(NT % 32 == 0 && 32 % LC == 0 && TW % 4 == 0 && TW <= 128, "shape");
 
   extern __shared__ __align__(1024) unsigned char smem[];
   uint32_t *box = reinterpret_cast<uint32_t *>(smem);
@@ -185,8 +187,8 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG>::min_bloc
     auto drain = [&](int cnt) {
       if (lane < cnt) {
         const unsigned long long e = q[(qh + lane) & (QCAP - 1)];
-        const int k = (int)(e >> 38);
-        const int ecl = (int)((e >> 32) & 63u);
+        const int k = (int)(e >> 39);
+        const int ecl = (int)((e >> 32) & 127u);
         const int er = (int)((e >> 16) & 0xFFFFu);
         const int ep = (int)(e & 0xFFFFu);
         const float ec = (float)(c0 + ecl);
@@ -199,7 +201,7 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG>::min_bloc
           for (int yy = er; yy < ep; yy++) sc[yy] = colour;
         } else {
           uint32_t *o = out + (size_t)er * W + c0 + ecl;
-          for (int yy = er; yy < ep; yy++, o += W) *o = colour;
+          for (int yy = er; yy < ep; yy++, o += W) __stcs(o, colour);
           if (colour == gap) col_flag[ecl] = 1;
         }
       }
@@ -209,39 +211,69 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG>::min_bloc
     for (int k0 = 0; k0 < n; k0 += CH) {
       if (__all_sync(FS_FULL_MASK, !valid || m == 0)) break;
       int r[U];
+      if constexpr (LC == 1) {
+        /* one lane per column: every lane is at the same depth, so the depth
+         * table loads are uniform and the occlusion test is a plain compare */
 #pragma unroll
-      for (int u = 0; u < U; u++) {
-        const int k = k0 + u * LC + dl;
-        int rr = H;
-        if (valid && m > 0 && k < n) {
-          const float4 L = __ldg(zl + k);
-          const float x = fa(L.x, fm(fcol, L.z));
-          const float y = fa(L.y, fm(fcol, L.w));
-          const float hh = HF ? height_bilinear(M, x, y) : height_nearest(M, x, y);
-          const float rel = fa(fm(fs(cam_h, hh), __ldg(zi + k)), horizon);
-          rr = min(max(f2i(rel), 0), H);
-          n_samples++;
+        for (int u = 0; u < U; u++) {
+          const int k = k0 + u;
+          int rr = H;
+          if (k < n) {
+            const float4 L = __ldg(zl + k);
+            const float iz = __ldg(zi + k);
+            if (valid && m > 0) {
+              const float x = fa(L.x, fm(fcol, L.z));
+              const float y = fa(L.y, fm(fcol, L.w));
+              const float hh = HF ? height_bilinear(M, x, y) : height_nearest(M, x, y);
+              rr = min(max(f2i(fa(fm(fs(cam_h, hh), iz), horizon)), 0), H);
+              n_samples++;
+            }
+          }
+          r[u] = rr;
         }
-        r[u] = rr;
-      }
 #pragma unroll
-      for (int u = 0; u < U; u++) {
-        int incl = r[u];
+        for (int u = 0; u < U; u++) {
+          const bool ev = r[u] < m;
+          const unsigned msk = __ballot_sync(FS_FULL_MASK, ev);
+          if (ev) q[(qt + __popc(msk & lanemask_lt)) & (QCAP - 1)] = pack_event(k0 + u, cl, r[u], m);
+          qt += __popc(msk);
+          m = min(m, r[u]);
+        }
+      } else {
 #pragma unroll
-        for (int off = 1; off < LC; off <<= 1) {
-          const int t = __shfl_up_sync(FS_FULL_MASK, incl, off, LC);
-          if (dl >= off) incl = min(incl, t);
+        for (int u = 0; u < U; u++) {
+          const int k = k0 + u * LC + dl;
+          int rr = H;
+          if (valid && m > 0 && k < n) {
+            const float4 L = __ldg(zl + k);
+            const float x = fa(L.x, fm(fcol, L.z));
+            const float y = fa(L.y, fm(fcol, L.w));
+            const float hh = HF ? height_bilinear(M, x, y) : height_nearest(M, x, y);
+            const float rel = fa(fm(fs(cam_h, hh), __ldg(zi + k)), horizon);
+            rr = min(max(f2i(rel), 0), H);
+            n_samples++;
+          }
+          r[u] = rr;
         }
-        const int excl = __shfl_up_sync(FS_FULL_MASK, incl, 1, LC);
-        const int prev = (dl == 0) ? m : min(m, excl);
-        const bool ev = r[u] < prev;
-        const unsigned msk = __ballot_sync(FS_FULL_MASK, ev);
-        if (ev) {
-          const int pos = (qt + __popc(msk & lanemask_lt)) & (QCAP - 1);
-          q[pos] = pack_event(k0 + u * LC + dl, cl, r[u], prev);
+#pragma unroll
+        for (int u = 0; u < U; u++) {
+          int incl = r[u];
+#pragma unroll
+          for (int off = 1; off < LC; off <<= 1) {
+            const int t = __shfl_up_sync(FS_FULL_MASK, incl, off, LC);
+            if (dl >= off) incl = min(incl, t);
+          }
+          const int excl = __shfl_up_sync(FS_FULL_MASK, incl, 1, LC);
+          const int prev = (dl == 0) ? m : min(m, excl);
+          const bool ev = r[u] < prev;
+          const unsigned msk = __ballot_sync(FS_FULL_MASK, ev);
+          if (ev) {
+            const int pos = (qt + __popc(msk & lanemask_lt)) & (QCAP - 1);
+            q[pos] = pack_event(k0 + u * LC + dl, cl, r[u], prev);
+          }
+          qt += __popc(msk);
+          m = min(m, __shfl_sync(FS_FULL_MASK, incl, LC - 1, LC));
         }
-        qt += __popc(msk);
-        m = min(m, __shfl_sync(FS_FULL_MASK, incl, LC - 1, LC));
       }
       __syncwarp();
       while (qt - qh >= 32) {
@@ -288,7 +320,7 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG>::min_bloc
       } else {
         for (int e = tid; e < H * TW; e += NT) {
           const int y = e / TW, cc = e - y * TW;
-          if (c0 + cc < W) out[(size_t)y * W + c0 + cc] = stage[cc * stride + y];
+          if (c0 + cc < W) __stcs(out + (size_t)y * W + c0 + cc, stage[cc * stride + y]);
         }
       }
     } else {
@@ -308,7 +340,7 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG>::min_bloc
       for (int c = 0; c < TW; c++) top = max(top, col_mf[c]);
       for (int e = tid; e < top * TW; e += NT) {
         const int y = e / TW, cc = e - y * TW;
-        if (c0 + cc < W && y < col_mf[cc]) out[(size_t)y * W + c0 + cc] = sky;
+        if (c0 + cc < W && y < col_mf[cc]) __stcs(out + (size_t)y * W + c0 + cc, sky);
       }
     }
     __syncthreads();
@@ -344,4 +376,9 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG>::min_bloc
   X(32, 8, 4, 0)        \
   X(32, 4, 4, 0)        \
   X(64, 4, 4, 0)        \
-  X(32, 4, 8, 0)
+  X(32, 4, 8, 0)        \
+  X(64, 2, 4, 0)        \
+  X(64, 1, 4, 0)        \
+  X(128, 1, 4, 0)       \
+  X(64, 1, 8, 0)        \
+  X(128, 1, 8, 0)

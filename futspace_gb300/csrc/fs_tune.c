@@ -17,8 +17,8 @@
 #include "fs_priv.h"
 
 static const FsTune k_batch_order[] = {
-    {8, 32, 1, 1, 0}, {8, 32, 2, 1, 0}, {16, 32, 2, 1, 0}, {32, 32, 1, 1, 0},
-    {4, 32, 2, 1, 0}, {32, 8, 4, 0, 0}, {32, 4, 4, 0, 0},  {8, 32, 2, 0, 0},
+    {64, 1, 4, 0, 0}, {64, 4, 4, 0, 0}, {32, 4, 4, 0, 0}, {8, 32, 1, 1, 0},
+    {8, 32, 2, 1, 0}, {16, 32, 2, 1, 0}, {32, 32, 1, 1, 0}, {8, 32, 2, 0, 0},
 };
 
 FsTune fs_default_batch_tune(fs_ctx *ctx, int32_t stride_max) {

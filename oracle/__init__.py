@@ -75,6 +75,8 @@ def lib():
             ("fso_render", i32, [P(OCamera), P(OParams), vp, vp, i32, i32, i32, i32, vp]),
             ("fso_render_mt", i32, [P(OCamera), P(OParams), vp, vp, i32, i32, i32, i32, vp, i32]),
             ("fso_max_threads", i32, []),
+            ("fso_render_split", i32, [P(OCamera), P(OParams), vp, i32, i32, vp, i32, i32, i32,
+                                       i32, vp, i32]),
             ("fso_shadowmap", i32, [vp, vp, i32, i32, vp, vp, i32]),
         ]:
             f = getattr(L, name)
@@ -108,7 +110,11 @@ def render(cam, params: OParams, heights: np.ndarray, colors: np.ndarray, width:
     c = np.ascontiguousarray(colors, np.uint32)
     out = np.empty((height, width), np.uint32)
     oc = to_ocam(cam)
-    if threads == 1:
+    if h.shape != c.shape:
+        rc = lib().fso_render_split(C.byref(oc), C.byref(params), h.ctypes.data, h.shape[0],
+                                    h.shape[1], c.ctypes.data, c.shape[0], c.shape[1], width,
+                                    height, out.ctypes.data, threads)
+    elif threads == 1:
         rc = lib().fso_render(C.byref(oc), C.byref(params), h.ctypes.data, c.ctypes.data,
                               h.shape[0], h.shape[1], width, height, out.ctypes.data)
     else:

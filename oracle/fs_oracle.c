@@ -187,12 +187,13 @@ static int fso_check(const fso_params *p, const uint8_t *hm, const uint32_t *cm,
 /* Samples one (z, column) pair: lines 218-226 (get_segment :63-66, the
  * samplers, the projection `i32.max 0 (i32.f32 relative_height)`). */
 static void fso_sample(const fso_camera *cam, const fso_params *p, const uint8_t *hm,
-                       const uint32_t *cm, int32_t MH, int32_t MW, const fso_line *l,
-                       float inv_z, int32_t i, uint32_t *colour, int32_t *row) {
+                       int32_t MH, int32_t MW, const uint32_t *cm, int32_t CH, int32_t CW,
+                       const fso_line *l, float inv_z, int32_t i, uint32_t *colour,
+                       int32_t *row) {
   float x = l->start_x + (float)i * l->end_x;
   float y = l->start_y + (float)i * l->end_y;
-  uint32_t c = p->color_filter == FSO_BILINEAR ? fso_color_bilinear(cm, MH, MW, x, y)
-                                               : fso_color_nearest(cm, MH, MW, x, y);
+  uint32_t c = p->color_filter == FSO_BILINEAR ? fso_color_bilinear(cm, CH, CW, x, y)
+                                               : fso_color_nearest(cm, CH, CW, x, y);
   float mh = p->height_filter == FSO_BILINEAR ? fso_height_bilinear(hm, MH, MW, x, y)
                                               : fso_height_nearest(hm, MH, MW, x, y);
   float height_diff = cam->height - mh;
@@ -233,9 +234,10 @@ static void fso_column(const uint32_t *cs, const int32_t *rs, int32_t n, int32_t
 }
 
 static int32_t fso_render_impl(const fso_camera *cam, const fso_params *p, const uint8_t *hm,
-                               const uint32_t *cm, int32_t MH, int32_t MW, int32_t W,
-                               int32_t H, uint32_t *out, int32_t threads) {
-  if (!cam || fso_check(p, hm, cm, MH, MW, W, H, out)) return -1;
+                               int32_t MH, int32_t MW, const uint32_t *cm, int32_t CH,
+                               int32_t CW, int32_t W, int32_t H, uint32_t *out,
+                               int32_t threads) {
+  if (!cam || fso_check(p, hm, cm, MH, MW, W, H, out) || CH <= 0 || CW <= 0) return -1;
   int32_t n = fso_num_depths(cam->distance, p->d, p->z0, p->floor_n);
   if (n < 1) return -2;
   float *zs = (float *)malloc(sizeof(float) * (size_t)n);
@@ -259,7 +261,7 @@ static int32_t fso_render_impl(const fso_camera *cam, const fso_params *p, const
     fso_line l = fso_get_h_line(zs[k], cam, W);
     float inv_z = (1.0f / zs[k]) * scale;
     for (int32_t i = 0; i < W; i++)
-      fso_sample(cam, p, hm, cm, MH, MW, &l, inv_z, i, &pc[(size_t)k * W + i],
+      fso_sample(cam, p, hm, MH, MW, cm, CH, CW, &l, inv_z, i, &pc[(size_t)k * W + i],
                  &pr[(size_t)k * W + i]);
   }
 
@@ -300,7 +302,7 @@ static int32_t fso_render_impl(const fso_camera *cam, const fso_params *p, const
 int32_t fso_render(const fso_camera *cam, const fso_params *p, const uint8_t *hm,
                    const uint32_t *cm, int32_t MH, int32_t MW, int32_t W, int32_t H,
                    uint32_t *out) {
-  return fso_render_impl(cam, p, hm, cm, MH, MW, W, H, out, 1);
+  return fso_render_impl(cam, p, hm, MH, MW, cm, MH, MW, W, H, out, 1);
 }
 
 int32_t fso_max_threads(void) {
@@ -315,7 +317,14 @@ int32_t fso_render_mt(const fso_camera *cam, const fso_params *p, const uint8_t 
                       const uint32_t *cm, int32_t MH, int32_t MW, int32_t W, int32_t H,
                       uint32_t *out, int32_t threads) {
   if (threads <= 0) threads = fso_max_threads();
-  return fso_render_impl(cam, p, hm, cm, MH, MW, W, H, out, threads);
+  return fso_render_impl(cam, p, hm, MH, MW, cm, MH, MW, W, H, out, threads);
+}
+
+int32_t fso_render_split(const fso_camera *cam, const fso_params *p, const uint8_t *hm,
+                         int32_t MH, int32_t MW, const uint32_t *cm, int32_t CH, int32_t CW,
+                         int32_t W, int32_t H, uint32_t *out, int32_t threads) {
+  if (threads <= 0) threads = fso_max_threads();
+  return fso_render_impl(cam, p, hm, MH, MW, cm, CH, CW, W, H, out, threads);
 }
 
 /* ---- shadowed colour map, generate_shadowmap_accumulated ------------------

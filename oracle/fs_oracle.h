@@ -66,6 +66,11 @@ int32_t fso_render_mt(const fso_camera *cam, const fso_params *p, const uint8_t 
                       const uint32_t *cm, int32_t MH, int32_t MW, int32_t W, int32_t H,
                       uint32_t *out, int32_t threads);
 int32_t fso_max_threads(void);
+/* Height map [MH][MW] and colour map [CH][CW] of different sizes (the
+ * interactive app samples the 1024x1024 shadowed colours over any height map). */
+int32_t fso_render_split(const fso_camera *cam, const fso_params *p, const uint8_t *hm,
+                         int32_t MH, int32_t MW, const uint32_t *cm, int32_t CH, int32_t CW,
+                         int32_t W, int32_t H, uint32_t *out, int32_t threads);
 
 /* Shadowed colour map, fut/effects.fut:108-125 (1024x1024 output, fixed). */
 int32_t fso_shadowmap(const uint8_t *hm, const uint32_t *cm, int32_t MH, int32_t MW,

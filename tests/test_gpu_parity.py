@@ -1,5 +1,5 @@
 """GPU parity: every frame the CUDA path renders equals the CPU oracle's, bit
-for bit (integer/byte output: no tolerance). Calls go through the C ABI."""
+for bit (ARGB u32 output: no tolerance). All calls go through the C ABI."""
 import numpy as np
 import pytest
 
@@ -10,27 +10,163 @@ pytestmark = pytest.mark.gpu
 FILTERS = [(h, c) for h in (0, 1) for c in (0, 1)]
 
 
-def _params(fs, **kw):
-    return fs.default_params(**kw)
+def _oracle(orc, cam, p, hm, cm, w, h):
+    return orc.render(cam, orc.params_from(p), hm, cm, w, h, threads=0)
 
 
 @pytest.mark.parametrize("hf,cf", FILTERS)
 def test_small_frames_all_filters(fs, orc, gpu_ctx, maps256, hf, cf):
     hm, cm = maps256
     fmap = fs.Map(gpu_ctx, hm, cm)
-    cams = fs.gen_cameras(31, hm, 6, above=(20, 80), distance=(150, 500), screen_h=48)
-    for cam in cams:
-        p = _params(fs, height_filter=hf, color_filter=cf)
+    p = fs.default_params(height_filter=hf, color_filter=cf)
+    for cam in fs.gen_cameras(31, hm, 6, above=(20, 80), distance=(150, 500), screen_h=48):
         got = gpu_ctx.render(fmap, cam, 64, 48, params=p)
-        ref = orc.render(cam, orc.params_from(p), hm, cm, 64, 48)
-        assert count_diff(got, ref) == 0
+        assert count_diff(got, _oracle(orc, cam, p, hm, cm, 64, 48)) == 0
 
 
-def test_config1_frame(fs, orc, gpu_ctx, maps1024):
-    """320x240, 1024^2 map, D=800 (n=1265), camera 40 above the local maximum."""
+def test_config1_frames(fs, orc, gpu_ctx, maps1024):
+    """320x240 over a 1024^2 map, D=800 (n=1265), 40 above the local maximum."""
     hm, cm = maps1024
     fmap = fs.Map(gpu_ctx, hm, cm)
+    p = fs.default_params()
     for cam in fs.gen_cameras(41, hm, 8, above=(40, 40), distance=(800, 800), screen_h=240):
         got = gpu_ctx.render(fmap, cam, 320, 240)
-        ref = orc.render(cam, orc.make_params(), hm, cm, 320, 240, threads=0)
-        assert count_diff(got, ref) == 0
+        assert count_diff(got, _oracle(orc, cam, p, hm, cm, 320, 240)) == 0
+
+
+def test_every_configuration(fs, orc, gpu_ctx, maps1024):
+    """Each compiled kernel configuration, on a TMA-aligned and an odd size."""
+    hm, cm = maps1024
+    fmap = fs.Map(gpu_ctx, hm, cm)
+    p = fs.default_params()
+    cams = fs.gen_cameras(51, hm, 2, above=(20, 120), distance=(300, 900), screen_h=120)
+    refs = {}
+    try:
+        for tune in fs.tune_table():
+            gpu_ctx.force_tune(tune)
+            for i, cam in enumerate(cams):
+                for (w, h) in ((160, 120), (157, 97)):
+                    key = (i, w, h)
+                    if key not in refs:
+                        refs[key] = _oracle(orc, cam, p, hm, cm, w, h)
+                    got = gpu_ctx.render(fmap, cam, w, h)
+                    assert count_diff(got, refs[key]) == 0, (tune, key)
+    finally:
+        gpu_ctx.force_tune(None)
+
+
+def test_walk_1080p_4096_map(fs, orc, gpu_ctx):
+    """The 64-frame camera walk at 1920x1080 over 4096^2 maps, D=3000, rendered
+    as one batch; every frame checked."""
+    hm = fs.gen_heights(7, 4096, 0.55)
+    cm = fs.gen_colors(8, hm, 12)
+    fmap = fs.Map(gpu_ctx, hm, cm)
+    walk = fs.gen_walk(9, hm, 64, step=2.0, yaw=0.02, above=(30, 120), distance=3000.0,
+                       screen_h=1080)
+    plan = fs.Plan(gpu_ctx, [fmap], [(c, 1920, 1080) for c in walk])
+    plan.run()
+    frames = plan.frames()
+    p = fs.default_params()
+    bad = [i for i, (c, f) in enumerate(zip(walk, frames))
+           if count_diff(f, _oracle(orc, c, p, hm, cm, 1920, 1080)) != 0]
+    assert not bad, f"frames differing from the oracle: {bad}"
+
+
+def _mixed_views(fs, hm, seed, n):
+    sizes = [(320, 240), (640, 480), (257, 131), (128, 96), (203, 64)]
+    rng = np.random.default_rng(seed)
+    out = []
+    for v in range(n):
+        w, h = sizes[int(rng.integers(0, len(sizes)))]
+        cam = fs.gen_cameras(seed * 100 + v, hm, 1, above=(20, 200), distance=(200, 1200),
+                             screen_h=h)[0]
+        out.append((cam, w, h))
+    return out
+
+
+def test_batch_plan_all_configurations(fs, orc, gpu_ctx, maps1024):
+    hm, cm = maps1024
+    fmap = fs.Map(gpu_ctx, hm, cm)
+    views = _mixed_views(fs, hm, 61, 24)
+    p = fs.default_params()
+    refs = [_oracle(orc, c, p, hm, cm, w, h) for c, w, h in views]
+    plan = fs.Plan(gpu_ctx, [fmap], views)
+    for tune in fs.tune_table():
+        plan.set_tune(*tune)
+        plan.run()
+        frames = plan.frames()
+        bad = [i for i, (f, r) in enumerate(zip(frames, refs)) if count_diff(f, r)]
+        assert not bad, (tune, bad)
+    plan.run_per_view()
+    assert all(count_diff(f, r) == 0 for f, r in zip(plan.frames(), refs))
+
+
+def test_batch_two_maps_and_camera_update(fs, orc, gpu_ctx, maps1024, maps256):
+    (h1, c1), (h2, c2) = maps1024, maps256
+    m1, m2 = fs.Map(gpu_ctx, h1, c1), fs.Map(gpu_ctx, h2, c2)
+    views = [(c, w, h, i % 2) for i, (c, w, h) in enumerate(_mixed_views(fs, h1, 71, 10))]
+    plan = fs.Plan(gpu_ctx, [m1, m2], views)
+    p = fs.default_params()
+    for step in range(2):
+        plan.run()
+        frames = plan.frames()
+        for (c, w, h, mi), f in zip(views, frames):
+            hm, cm = (h1, c1) if mi == 0 else (h2, c2)
+            assert count_diff(f, _oracle(orc, c, p, hm, cm, w, h)) == 0
+        # move every camera; draw distances shrink so the depth tables still fit
+        new = []
+        for c, w, h, mi in views:
+            c2_ = fs.Camera(*c.as_tuple())
+            c2_.x += 3.5
+            c2_.angle += 0.25
+            c2_.distance *= 0.9
+            new.append((c2_, w, h, mi))
+        plan.set_cameras([v[0] for v in new])
+        views = new
+
+
+@pytest.mark.parametrize("hf,cf", FILTERS)
+@pytest.mark.parametrize("gap", [0, 1])
+def test_adversarial_inputs(fs, orc, gpu_ctx, maps256, hf, cf, gap):
+    """Zero-colour and sky-colour texels, integral and negative coordinates,
+    cameras below or exactly at the terrain (z = 0 hazards), both gap rules."""
+    hm, cm = maps256
+    cm = cm.copy()
+    cm[::3, ::2] = 0
+    cm[1::5, 1::3] = 0xFF9090E0
+    fmap = fs.Map(gpu_ctx, hm, cm)
+    p = fs.default_params(height_filter=hf, color_filter=cf, gap_rule=gap)
+    at = orc.lib().fso_height_bilinear(hm.ctypes.data, 256, 256, 64.5, 64.25)
+    cams = [dict(x=100.0, y=100.0, height=300.0, angle=0.0, horizon=24.0, distance=200.0),
+            dict(x=-37.0, y=-300.0, height=120.0, angle=1.5707964, horizon=30.0,
+                 distance=400.0),
+            dict(x=64.5, y=64.25, height=-10.0, angle=0.3, horizon=24.0, distance=150.0),
+            dict(x=64.5, y=64.25, height=at, angle=0.3, horizon=24.0, distance=150.0)]
+    for c in cams:
+        cam = fs.Camera(c["x"], c["y"], c["height"], c["angle"], c["horizon"], c["distance"],
+                        1.2, 0xFF9090E0)
+        got = gpu_ctx.render(fmap, cam, 61, 47, params=p)
+        assert count_diff(got, _oracle(orc, cam, p, hm, cm, 61, 47)) == 0
+
+
+def test_mode_b_and_custom_scale(fs, orc, gpu_ctx, maps256):
+    """tests/futspace.fut parameters: nearest, z0=1, d=0.005, scale 240, gap=sky."""
+    hm, cm = maps256
+    fmap = fs.Map(gpu_ctx, hm, cm)
+    p = fs.default_params(invz_param1=0.005, invz_param2=1.0, magic_number=240.0,
+                          height_filter=0, color_filter=0, gap_rule=1, floor_n=0)
+    cam = fs.Camera(128.0, 200.0, 78.0, 0.0, 100.0, 800.0, 1.0, 0xFF9090E0)
+    got = gpu_ctx.render(fmap, cam, 800, 400, params=p)
+    assert count_diff(got, _oracle(orc, cam, p, hm, cm, 800, 400)) == 0
+
+
+def test_non_power_of_two_map_and_i32_heights(fs, orc, gpu_ctx):
+    hm = fs.gen_heights(3, 512, 0.6)[:300, :200].copy()
+    cm = fs.gen_colors(4, hm, 12)
+    # i32 heights with junk above bit 7: update_map keeps `elem & 0xFF`
+    hi = hm.astype(np.int32) | (np.int32(0x5A) << 8)
+    fmap = fs.Map(gpu_ctx, hi, cm)
+    p = fs.default_params()
+    for cam in fs.gen_cameras(9, hm, 3, above=(30, 60), distance=(300, 700), screen_h=90):
+        got = gpu_ctx.render(fmap, cam, 120, 90)
+        assert count_diff(got, _oracle(orc, cam, p, hm, cm, 120, 90)) == 0
