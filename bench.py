@@ -234,6 +234,7 @@ def main():
 
     import torch
     import futspace_gb300 as fs
+    from futspace_gb300 import replicas
 
     dist = None
     if world > 1:
@@ -331,12 +332,10 @@ def main():
                "ms_per_step": e2e_ms}
 
     ms = float(np.mean(t_batch))
-    ms_max = ms
-    if dist:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
-    value = px * world / ms_max / 1e6
+    # replicas: every rank renders its own views; sum pixels, slowest rank's time
+    agg = replicas.aggregate(px, ms, dist=dist, device=f"cuda:{local}")
+    ms_max = agg["ms"]
+    value = agg["gpix_s"]
 
     peaks = measured_peaks()
     vb = view_bytes(views, samples, events)

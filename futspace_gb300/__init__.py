@@ -116,6 +116,7 @@ def lib():
     _sig(L, "fs_ctx_kernel_launches", i64, [vp])
     _sig(L, "fs_ctx_stats", C.c_int, [vp, i32, P(u64)])
     _sig(L, "fs_ctx_force_tune", C.c_int, [vp, P(i32)])
+    _sig(L, "fs_ctx_set_option", C.c_int, [vp, C.c_char_p, i64])
     _sig(L, "fs_map_new", C.c_int, [vp, P(vp), vp, vp, i64, i64])
     _sig(L, "fs_map_new_i32", C.c_int, [vp, P(vp), vp, vp, i64, i64])
     _sig(L, "fs_map_wrap_device", C.c_int, [vp, P(vp), vp, vp, i64, i64])
@@ -262,6 +263,9 @@ class Context:
     @property
     def launches(self) -> int:
         return lib().fs_ctx_kernel_launches(self._h)
+
+    def set_option(self, name: str, value: int):
+        self.check(lib().fs_ctx_set_option(self._h, name.encode(), int(value)), "set_option")
 
     def force_tune(self, tune=None):
         """tune = (tile_width, lanes_per_column, depth_per_lane, stage) or None."""

@@ -165,6 +165,8 @@ int fs_ctx_new(fs_ctx **out, int32_t device) {
   ctx->use_tma = ctx->encode != NULL;
   const char *env = getenv("FS_NO_TMA");
   if (env && env[0] == '1') ctx->use_tma = 0;
+  env = getenv("FS_NO_SKIP");
+  if (env && env[0] == '1') ctx->no_skip = 1;
   if (cudaMalloc((void **)&ctx->stats_dev, 2 * sizeof(unsigned long long)) != cudaSuccess) {
     ctx->broken = 1;
     *out = ctx;
@@ -205,6 +207,18 @@ int fs_ctx_set_stream(fs_ctx *ctx, void *stream) {
 void *fs_ctx_get_stream(fs_ctx *ctx) { return ctx ? (void *)ctx->stream : NULL; }
 
 int64_t fs_ctx_kernel_launches(fs_ctx *ctx) { return ctx ? ctx->launches : 0; }
+
+int fs_ctx_set_option(fs_ctx *ctx, const char *name, int64_t value) {
+  if (!ctx || !name) return FS_ERR_ARG;
+  if (!strcmp(name, "skip")) {
+    ctx->no_skip = value ? 0 : 1;
+  } else if (!strcmp(name, "tma")) {
+    ctx->use_tma = (value && ctx->encode) ? 1 : 0;
+  } else {
+    return fs_fail(ctx, FS_ERR_ARG, "unknown option '%s'", name);
+  }
+  return FS_OK;
+}
 
 int fs_ctx_force_tune(fs_ctx *ctx, const int32_t tune5[5]) {
   if (!ctx) return FS_ERR_ARG;
@@ -275,6 +289,19 @@ int fs_encode_frame_map(fs_ctx *ctx, uint32_t *frame, int32_t W, int32_t H, int3
 
 static int is_pow2(int64_t v) { return v > 0 && (v & (v - 1)) == 0; }
 
+/* Builds the height max pyramid after the quads (same stream). */
+static int fs_map_build_pyramid(fs_ctx *ctx, fs_map *m) {
+  const size_t bytes = fs_pyramid_layout(&m->dev);
+  if (!bytes) return 0;
+  if (cudaMalloc((void **)&m->pyr, bytes) != cudaSuccess) {
+    m->pyr = NULL;
+    m->dev.pyr = NULL;
+    return (int)cudaErrorMemoryAllocation;
+  }
+  m->dev.pyr = m->pyr;
+  return fsk_build_pyramid(&m->dev, m->pyr, ctx->stream);
+}
+
 static int fs_map_alloc(fs_ctx *ctx, fs_map **out, int64_t rows, int64_t cols) {
   if (!ctx || !out) return fs_fail(ctx, FS_ERR_ARG, "NULL argument");
   if (rows <= 0 || cols <= 0 || rows > 65536 || cols > 65536)
@@ -314,6 +341,7 @@ int fs_map_new(fs_ctx *ctx, fs_map **out, const uint8_t *heights, const uint32_t
   int e = cudaMalloc((void **)&tmp, cnt);
   if (!e) e = cudaMemcpyAsync(tmp, heights, cnt, cudaMemcpyHostToDevice, ctx->stream);
   if (!e) e = fsk_build_quads(tmp, m->q, (int32_t)rows, (int32_t)cols, ctx->stream);
+  if (!e) e = fs_map_build_pyramid(ctx, m);
   if (!e) e = cudaMemcpyAsync(m->c, colors, cnt * 4, cudaMemcpyHostToDevice, ctx->stream);
   if (!e) e = cudaStreamSynchronize(ctx->stream);
   cudaFree(tmp);
@@ -339,6 +367,7 @@ int fs_map_new_i32(fs_ctx *ctx, fs_map **out, const int32_t *heights, const uint
   if (!e) e = cudaMemcpyAsync(tmp, heights, cnt * 4, cudaMemcpyHostToDevice, ctx->stream);
   if (!e) e = fsk_mask_heights(tmp, h8, (int64_t)cnt, ctx->stream);
   if (!e) e = fsk_build_quads(h8, m->q, (int32_t)rows, (int32_t)cols, ctx->stream);
+  if (!e) e = fs_map_build_pyramid(ctx, m);
   if (!e) e = cudaMemcpyAsync(m->c, colors, cnt * 4, cudaMemcpyHostToDevice, ctx->stream);
   if (!e) e = cudaStreamSynchronize(ctx->stream);
   cudaFree(tmp);
@@ -375,6 +404,7 @@ int fs_map_wrap_device(fs_ctx *ctx, fs_map **out, const uint8_t *heights_dev,
   m->dev.MW = m->dev.CW = (int32_t)cols;
   m->dev.pow2 = m->dev.cpow2 = is_pow2(rows) && is_pow2(cols);
   int e = fsk_build_quads(heights_dev, m->q, (int32_t)rows, (int32_t)cols, ctx->stream);
+  if (!e) e = fs_map_build_pyramid(ctx, m);
   if (!e) e = cudaStreamSynchronize(ctx->stream);
   if (e) {
     fs_map_free(ctx, m);
@@ -388,6 +418,7 @@ int fs_map_free(fs_ctx *ctx, fs_map *map) {
   if (!map) return FS_OK;
   if (ctx) cudaSetDevice(ctx->device);
   if (map->owned) cudaFree(map->q);
+  cudaFree(map->pyr);
   if (map->owned == 1) cudaFree(map->c);
   free(map);
   return FS_OK;
@@ -465,6 +496,7 @@ int fs_render_view(fs_ctx *ctx, const FsMapDev *map, FsView *v, const FsTune *tu
   }
   L->view0 = *v;
   L->maps[0] = *map;
+  if (ctx->no_skip) L->maps[0].pyr = NULL;
   L->view0.map = 0;
   L->zline = zline;
   L->zinvz = zinvz;

@@ -22,6 +22,8 @@ extern "C" {
 #define FS_MAX_DEPTHS (1 << 20)
 /* Maps bound to one launch. */
 #define FS_MAX_MAPS 4
+/* Levels of the height max pyramid (2^16 texels per side). */
+#define FS_PYR_MAX 16
 
 /* Filter flags of a view. */
 #define FSV_HEIGHT_BILINEAR 1
@@ -54,6 +56,12 @@ typedef struct {
                          1024x1024 shadowed colour map over any height map) */
   int32_t pow2;       /* MH and MW are powers of two: wrap with a mask */
   int32_t cpow2;      /* CH and CW are powers of two */
+  /* Max pyramid of the heights (power-of-two maps only; NULL: none). Level l
+   * (1..pyr_levels) has (MH>>l) x (MW>>l) u8 cells, each the maximum height of
+   * its 2^l x 2^l texels, stored at pyr + pyr_off[l-1]. */
+  const uint8_t *pyr;
+  int32_t pyr_levels;
+  int32_t pyr_off[FS_PYR_MAX];
 } FsMapDev;
 
 /* Everything one render launch needs, passed by value (__grid_constant__), so
@@ -95,6 +103,11 @@ int fsk_tune_supported(const FsTune *t);
 int fsk_shadowmap(const FsMapDev *map, const float sun[3], uint32_t *out, cudaStream_t st);
 int fsk_mask_heights(const int32_t *in, uint8_t *out, int64_t count, cudaStream_t st);
 int fsk_build_quads(const uint8_t *h, uint32_t *q, int32_t MH, int32_t MW, cudaStream_t st);
+/* Builds the max pyramid of M (M->q, MH, MW set; pyr, levels, offsets filled). */
+int fsk_build_pyramid(const FsMapDev *M, uint8_t *pyr, cudaStream_t st);
+/* Bytes of the max pyramid of a map; fills levels and offsets into *M. 0 when
+ * the map is not power-of-two sized. */
+size_t fs_pyramid_layout(FsMapDev *M);
 
 #ifdef __cplusplus
 }

@@ -138,6 +138,56 @@ extern "C" size_t fsk_render_smem(const FsTune *t, int32_t stride_max) {
   return box + nw * queue_cap(t->u) * 8 + 256 * 4 + (size_t)t->tw * 8 + stage;
 }
 
+/* Level 1 of the max pyramid: each cell is the maximum of the 2x2 texels that
+ * quad (2y, 2x) packs. */
+__global__ void pyr1_kernel(const uint32_t *q, int MW, uint8_t *out, int ch, int cw) {
+  const int y = blockIdx.y;
+  for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < cw; x += gridDim.x * blockDim.x) {
+    const uint32_t v = q[(size_t)(2 * y) * MW + 2 * x];
+    const uint32_t a = max(v & 0xFFu, (v >> 8) & 0xFFu), b = max((v >> 16) & 0xFFu, v >> 24);
+    out[(size_t)y * cw + x] = (uint8_t)max(a, b);
+  }
+}
+
+/* Level l+1 from level l: maximum of 2x2 cells. */
+__global__ void pyr_kernel(const uint8_t *in, int iw, uint8_t *out, int ch, int cw) {
+  const int y = blockIdx.y;
+  for (int x = blockIdx.x * blockDim.x + threadIdx.x; x < cw; x += gridDim.x * blockDim.x) {
+    const uint8_t *r0 = in + (size_t)(2 * y) * iw + 2 * x;
+    const uint8_t *r1 = r0 + iw;
+    out[(size_t)y * cw + x] = (uint8_t)max(max(r0[0], r0[1]), max(r1[0], r1[1]));
+  }
+}
+
+extern "C" size_t fs_pyramid_layout(FsMapDev *M) {
+  M->pyr = nullptr;
+  M->pyr_levels = 0;
+  if (!M->pow2 || M->MH < 4 || M->MW < 4) return 0;
+  size_t off = 0;
+  int l = 1;
+  for (; l <= FS_PYR_MAX && (M->MH >> l) >= 1 && (M->MW >> l) >= 1; l++) {
+    M->pyr_off[l - 1] = (int32_t)off;
+    off += (size_t)(M->MH >> l) * (size_t)(M->MW >> l);
+  }
+  M->pyr_levels = l - 1;
+  return off;
+}
+
+extern "C" int fsk_build_pyramid(const FsMapDev *M, uint8_t *pyr, cudaStream_t st) {
+  for (int l = 1; l <= M->pyr_levels; l++) {
+    const int ch = M->MH >> l, cw = M->MW >> l;
+    const int bx = cw < 256 ? 1 : (cw / 256 > 16 ? 16 : cw / 256);
+    if (l == 1)
+      pyr1_kernel<<<dim3(bx, ch), 256, 0, st>>>(M->q, M->MW, pyr + M->pyr_off[0], ch, cw);
+    else
+      pyr_kernel<<<dim3(bx, ch), 256, 0, st>>>(pyr + M->pyr_off[l - 2], M->MW >> (l - 1),
+                                               pyr + M->pyr_off[l - 1], ch, cw);
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return (int)e;
+  }
+  return (int)cudaSuccess;
+}
+
 extern "C" int fsk_build_quads(const uint8_t *h, uint32_t *q, int32_t MH, int32_t MW,
                                cudaStream_t st) {
   if (MH <= 0 || MW <= 0) return (int)cudaErrorInvalidValue;

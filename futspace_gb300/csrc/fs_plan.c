@@ -55,7 +55,10 @@ void fs_plan_free(fs_plan *p) {
 
 static void plan_fill_launch(fs_plan *p, FsLaunch *L) {
   memset(L, 0, sizeof(*L));
-  for (int i = 0; i < p->nmaps; i++) L->maps[i] = p->maps[i];
+  for (int i = 0; i < p->nmaps; i++) {
+    L->maps[i] = p->maps[i];
+    if (p->ctx->no_skip) L->maps[i].pyr = NULL;
+  }
   L->views = p->fv_d;
   L->items = p->items_d;
   L->tmaps = p->tm_d;

@@ -26,6 +26,7 @@ struct fs_ctx {
   int32_t has_err;
   void *encode; /* cuTensorMapEncodeTiled, NULL when the driver lacks it */
   int32_t use_tma;
+  int32_t no_skip; /* 1: ignore the height max pyramid (no chunk skipping) */
   int32_t sm_count;
   size_t smem_optin;
   float4 *zline; /* single-frame depth table */
@@ -45,6 +46,7 @@ struct fs_ctx {
 struct fs_map {
   FsMapDev dev;
   int32_t owned; /* 1: quads and colours owned; 2: quads owned, colours borrowed */
+  uint8_t *pyr;  /* height max pyramid (owned), NULL when not built */
   uint32_t *q;
   uint32_t *c;
   int64_t rows, cols;

@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG>::min_bloc
     const float cam_h = Vp->cam_h, horizon = Vp->horizon;
     const int W = Vp->W, H = Vp->H, n = Vp->n;
     const uint32_t sky = Vp->sky, gap = Vp->gap;
-    const FsMapDev M = P.maps[Vp->map];
+    const FsMapDev &M = P.maps[Vp->map]; /* read in place: no local copy to index */
     const float4 *zl = P.zline + Vp->zoff;
     const float *zi = P.zinvz + Vp->zoff;
     uint32_t *const out = Vp->out;
@@ -210,6 +210,26 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG>::min_bloc
 
     for (int k0 = 0; k0 < n; k0 += CH) {
       if (__all_sync(FS_FULL_MASK, !valid || m == 0)) break;
+      if (M.pyr) {
+        /* Exact skip: rows are monotone in the height and in inv_z, so a row
+         * computed from an upper bound of every height in the chunk, at the
+         * chunk's nearest or farthest depth, bounds every sample's row from
+         * below. If that bound is not above the running minimum, no sample of
+         * the chunk can be an event for this column. */
+        const int ka = k0, kb = min(k0 + CH, n) - 1;
+        const float4 La = __ldg(zl + ka), Lb = __ldg(zl + kb);
+        const float iza = __ldg(zi + ka), izb = __ldg(zi + kb);
+        bool skip = !valid || m == 0;
+        if (!skip) {
+          const float xa = fa(La.x, fm(fcol, La.z)), ya = fa(La.y, fm(fcol, La.w));
+          const float xb = fa(Lb.x, fm(fcol, Lb.z)), yb = fa(Lb.y, fm(fcol, Lb.w));
+          const float dh = fs(cam_h, fa((float)segment_max_height(M, xa, ya, xb, yb), 1.0f));
+          const int ra = min(max(f2i(fa(fm(dh, iza), horizon)), 0), H);
+          const int rb = min(max(f2i(fa(fm(dh, izb), horizon)), 0), H);
+          skip = min(ra, rb) >= m;
+        }
+        if (__all_sync(FS_FULL_MASK, skip)) continue;
+      }
       int r[U];
       if constexpr (LC == 1) {
         /* one lane per column: every lane is at the same depth, so the depth

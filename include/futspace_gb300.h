@@ -101,6 +101,12 @@ int64_t fs_ctx_kernel_launches(fs_ctx *ctx);
  * fs_ctx_force_tune fixes the configuration of every following single-frame
  * render; NULL or tile width 0 restores the tuning-cache / default choice. */
 int fs_ctx_force_tune(fs_ctx *ctx, const int32_t tune5[5]);
+/* Context options: "skip" (1, default: skip depth chunks that a max-pyramid
+ * bound proves cannot change the frame; 0: march every depth sample) and "tma"
+ * (1, default when the driver provides tensor maps: TMA row stores from the
+ * staged kernels; 0: plain stores). Plans capture the options at creation or
+ * retuning. Pixels are identical either way. */
+int fs_ctx_set_option(fs_ctx *ctx, const char *name, int64_t value);
 
 /* ---- maps ---------------------------------------------------------------- */
 /* Copies a [rows][cols] u8 height map and ARGB colour map from host memory to

@@ -170,3 +170,31 @@ def test_non_power_of_two_map_and_i32_heights(fs, orc, gpu_ctx):
     for cam in fs.gen_cameras(9, hm, 3, above=(30, 60), distance=(300, 700), screen_h=90):
         got = gpu_ctx.render(fmap, cam, 120, 90)
         assert count_diff(got, _oracle(orc, cam, p, hm, cm, 120, 90)) == 0
+
+
+def test_chunk_skip_is_exact_and_saves_work(fs, orc, gpu_ctx):
+    """The max-pyramid chunk skip changes no pixel and evaluates fewer samples."""
+    hm = fs.gen_heights(17, 1024, 0.55)
+    cm = fs.gen_colors(18, hm, 12)
+    fmap = fs.Map(gpu_ctx, hm, cm)
+    views = _mixed_views(fs, hm, 81, 12)
+    p = fs.default_params()
+    counts = {}
+    for skip in (0, 1):
+        gpu_ctx.set_option("skip", skip)
+        try:
+            for tune in fs.tune_table():
+                gpu_ctx.force_tune(tune)
+                gpu_ctx.stats(True)
+                for c, w, h in views:
+                    got = gpu_ctx.render(fmap, c, w, h)
+                    assert count_diff(got, _oracle(orc, c, p, hm, cm, w, h)) == 0, (skip, tune)
+                counts[(skip, tune)] = gpu_ctx.stats(True)
+        finally:
+            gpu_ctx.force_tune(None)
+            gpu_ctx.set_option("skip", 1)
+    for tune in fs.tune_table():
+        s_off, e_off = counts[(0, tune)]
+        s_on, e_on = counts[(1, tune)]
+        assert e_on == e_off          # the same occlusion events are coloured
+        assert s_on < s_off           # fewer depth samples are evaluated
