@@ -55,6 +55,30 @@ class Params(C.Structure):
                 ("reserved", C.c_int32)]
 
 
+class Request(C.Structure):
+    """fs_request: one render request of a serving session."""
+    _fields_ = [("session", C.c_int32), ("map", C.c_int32), ("width", C.c_int32),
+                ("height", C.c_int32), ("cam", Camera), ("host_out", C.c_void_p),
+                ("arrival_ns", C.c_int64), ("start_ns", C.c_int64), ("done_ns", C.c_int64),
+                ("status", C.c_int32), ("batch", C.c_int32)]
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("budget_bytes", C.c_int64), ("nsessions", C.c_int32), ("max_batch", C.c_int32),
+                ("slots", C.c_int32), ("max_depths", C.c_int32), ("tune", C.c_int32 * 5)]
+
+
+class ServeStats(C.Structure):
+    _fields_ = [("wall_s", C.c_double), ("gpix_s", C.c_double), ("p50_ms", C.c_double),
+                ("p99_ms", C.c_double), ("mean_ms", C.c_double), ("max_ms", C.c_double),
+                ("requests", C.c_int64), ("pixels", C.c_int64), ("batches", C.c_int64),
+                ("mean_batch", C.c_double), ("peak_arena_bytes", C.c_int64),
+                ("max_inflight", C.c_int32), ("errors", C.c_int32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class View(C.Structure):
     _fields_ = [("cam", Camera), ("width", C.c_int32), ("height", C.c_int32),
                 ("map", C.c_int32), ("reserved", C.c_int32)]
@@ -73,7 +97,7 @@ _LIVE: "weakref.WeakSet" = weakref.WeakSet()
 
 def _release_all():
     objs = list(_LIVE)
-    for kind in (Plan, Map, Context):
+    for kind in (Server, Plan, PinnedBuffer, Map, Context):
         for o in objs:
             if isinstance(o, kind):
                 try:
@@ -144,6 +168,11 @@ def lib():
     _sig(L, "fs_plan_autotune", C.c_int, [vp, i32, P(i32), P(f32)])
     _sig(L, "fs_tune_count", C.c_int, [])
     _sig(L, "fs_tune_get", C.c_int, [C.c_int, P(i32)])
+    _sig(L, "fs_host_alloc", vp, [C.c_size_t])
+    _sig(L, "fs_host_free", None, [vp])
+    _sig(L, "fs_server_new", C.c_int, [vp, P(vp), P(vp), i32, P(Params), P(ServerConfig)])
+    _sig(L, "fs_server_free", None, [vp])
+    _sig(L, "fs_server_run", C.c_int, [vp, P(Request), i32, i32, P(ServeStats)])
     _sig(L, "fsgen_heights", C.c_int, [u64, i32, f32, vp])
     _sig(L, "fsgen_colors", C.c_int, [u64, vp, i64, i32, vp])
     _sig(L, "fsgen_local_max", i32, [vp, i32, i32, f32, f32])
@@ -442,6 +471,75 @@ class Plan:
     def close(self):
         if self._h:
             lib().fs_plan_free(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        if _finalizing():
+            return
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class PinnedBuffer:
+    """Page-locked host memory viewed as a numpy array (fs_host_alloc)."""
+
+    def __init__(self, shape, dtype=np.uint32):
+        nbytes = int(np.prod(shape)) * np.dtype(dtype).itemsize
+        self._p = lib().fs_host_alloc(nbytes)
+        if not self._p:
+            raise FsError(4, "fs_host_alloc")
+        self.array = np.ctypeslib.as_array((C.c_uint8 * nbytes).from_address(self._p))
+        self.array = self.array.view(dtype).reshape(shape)
+        _LIVE.add(self)
+
+    @property
+    def ptr(self) -> int:
+        return self._p
+
+    def close(self):
+        if self._p:
+            self.array = None
+            lib().fs_host_free(self._p)
+            self._p = None
+
+    def __del__(self):
+        if _finalizing():
+            return
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """fs_server: continuous-batching request loop over the persistent kernel."""
+
+    def __init__(self, ctx: Context, maps: Sequence[Map], budget_bytes: int, nsessions: int,
+                 max_batch: int = 64, slots: int = 3, max_distance: float = 3000.0,
+                 tune=None, params: Params | None = None):
+        self.ctx = ctx
+        self._h = C.c_void_p()
+        self.params = params or default_params()
+        cfg = ServerConfig(budget_bytes, nsessions, max_batch, slots,
+                           num_depths(max_distance, self.params))
+        for i, v in enumerate(tuple(tune or ()) + (0,) * (5 - len(tuple(tune or ())))):
+            cfg.tune[i] = v
+        mp = (C.c_void_p * len(maps))(*[m.handle.value for m in maps])
+        ctx.check(lib().fs_server_new(ctx.handle, C.byref(self._h), mp, len(maps),
+                                      C.byref(self.params), C.byref(cfg)), "fs_server_new")
+        _LIVE.add(self)
+
+    def run(self, requests, realtime: bool = False) -> dict:
+        st = ServeStats()
+        self.ctx.check(lib().fs_server_run(self._h, requests, len(requests), int(realtime),
+                                           C.byref(st)), "fs_server_run")
+        return st.as_dict()
+
+    def close(self):
+        if self._h:
+            lib().fs_server_free(self._h)
             self._h = C.c_void_p()
 
     def __del__(self):

@@ -285,6 +285,16 @@ int fs_encode_frame_map(fs_ctx *ctx, uint32_t *frame, int32_t W, int32_t H, int3
   return r == CUDA_SUCCESS ? 1 : 0;
 }
 
+void *fs_host_alloc(size_t bytes) {
+  void *p = NULL;
+  if (cudaMallocHost(&p, bytes ? bytes : 1) != cudaSuccess) return NULL;
+  return p;
+}
+
+void fs_host_free(void *p) {
+  if (p) cudaFreeHost(p);
+}
+
 /* ---- maps -------------------------------------------------------------------- */
 
 static int is_pow2(int64_t v) { return v > 0 && (v & (v - 1)) == 0; }

@@ -28,8 +28,7 @@ namespace {
 /* Per depth k (z = z_{k+1}): get_zs (fut/voxel_renderer.fut:34), get_h_line
  * (:43-60) and inv_z = (1/z) * scale (:217). The reference evaluates these once
  * per depth slice in its outer map (:215-217); so does this table. */
-__global__ void ztable_kernel(const FsView *views, FsView view0, float4 *zline, float *zinvz) {
-  const FsView *Vp = views ? views + blockIdx.y : &view0;
+__device__ __forceinline__ void ztable_fill(const FsView *Vp, float4 *zline, float *zinvz) {
   const int n = Vp->n;
   const float d = Vp->d, z0 = Vp->z0, s = Vp->sa, c = Vp->ca, v = Vp->fov;
   const float fw = (float)Vp->W;
@@ -48,6 +47,19 @@ __global__ void ztable_kernel(const FsView *views, FsView view0, float4 *zline, 
     zl[k] = make_float4(fa(lx, Vp->cam_x), fa(ly, Vp->cam_y), dx, dy);
     zi[k] = fm(fd(1.0f, z), Vp->scale);
   }
+}
+
+__global__ void ztable_kernel(const FsView *views, FsView view0, float4 *zline, float *zinvz) {
+  ztable_fill(views ? views + blockIdx.y : &view0, zline, zinvz);
+}
+
+/* Serving launch prologue: record i of the packed launch goes to the session
+ * table at ids[i], and its depth table is built. */
+__global__ void serve_prepare_kernel(const FsView *packed, const int32_t *ids, FsView *sess,
+                                     float4 *zline, float *zinvz) {
+  const FsView *Vp = packed + blockIdx.y;
+  if (blockIdx.x == 0 && threadIdx.x == 0) sess[ids[blockIdx.y]] = *Vp;
+  ztable_fill(Vp, zline, zinvz);
 }
 
 /* generate_shadowmap_accumulated, fut/effects.fut:108-125, with the nearest
@@ -119,6 +131,16 @@ extern "C" int fsk_ztable(const FsView *views_dev, const FsView *view0, int32_t 
   else memset(&v0, 0, sizeof(v0));
   dim3 grid(bx, views_dev ? nviews : 1);
   ztable_kernel<<<grid, threads, 0, st>>>(views_dev, v0, zline, zinvz);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int fsk_serve_prepare(const FsView *packed_dev, const int32_t *ids_dev, int32_t nb,
+                                 int32_t max_n, FsView *sess_dev, float4 *zline, float *zinvz,
+                                 cudaStream_t st) {
+  if (nb <= 0 || max_n <= 0) return (int)cudaSuccess;
+  int bx = (max_n + 255) / 256;
+  if (bx > 64) bx = 64;
+  serve_prepare_kernel<<<dim3(bx, nb), 256, 0, st>>>(packed_dev, ids_dev, sess_dev, zline, zinvz);
   return (int)cudaGetLastError();
 }
 

@@ -108,6 +108,11 @@ int fs_ctx_force_tune(fs_ctx *ctx, const int32_t tune5[5]);
  * retuning. Pixels are identical either way. */
 int fs_ctx_set_option(fs_ctx *ctx, const char *name, int64_t value);
 
+/* Page-locked host memory (cudaMallocHost) for frame downloads that should not
+ * block the calling thread, e.g. fs_request.host_out. */
+void *fs_host_alloc(size_t bytes);
+void fs_host_free(void *p);
+
 /* ---- maps ---------------------------------------------------------------- */
 /* Copies a [rows][cols] u8 height map and ARGB colour map from host memory to
  * the device. The maps stay resident until fs_map_free. */
@@ -188,6 +193,57 @@ int fs_tune_get(int i, int32_t out5[5]);
  * the depth samples it evaluated and the occlusion events it coloured. Reading
  * (out2 != NULL) waits for the stream and resets the counters. */
 int fs_ctx_stats(fs_ctx *ctx, int32_t enable, uint64_t out2[2]);
+
+/* ---- serving: continuous batching of render requests -----------------------
+ * A server keeps the maps and one view record per session resident on the
+ * device. Requests arrive over time; each is admitted when its session has no
+ * request in flight and its frame fits in the free part of a device
+ * framebuffer arena of `budget_bytes`. Admitted requests are launched in
+ * batches -- every admitted request that is ready when a launch slot frees up
+ * -- through the same persistent kernel, with up to `slots` batches in flight
+ * on separate streams, so new work overlaps work already on the GPU. A frame's
+ * memory returns to the arena when its request completes. Pixels do not depend
+ * on batching: a frame rendered alone equals the same frame rendered in a mix. */
+typedef struct {
+  int64_t budget_bytes; /* device framebuffer arena */
+  int32_t nsessions;
+  int32_t max_batch;    /* requests per launch */
+  int32_t slots;        /* launches in flight */
+  int32_t max_depths;   /* depth capacity per session (fs_num_depths of the largest distance) */
+  int32_t tune[5];      /* kernel configuration; tile width 0 = default */
+} fs_server_config;
+
+typedef struct {
+  int32_t session, map;  /* session id in [0, nsessions); map index */
+  int32_t width, height;
+  fs_camera cam;
+  uint32_t *host_out;    /* if not NULL the frame is copied here before completion */
+  int64_t arrival_ns;    /* release time, relative to the start of fs_server_run */
+  int64_t start_ns;      /* filled: launch time */
+  int64_t done_ns;       /* filled: completion time (frame in device memory or host_out) */
+  int32_t status;        /* filled: FS_OK or an error code */
+  int32_t batch;         /* filled: index of the launch that rendered it */
+} fs_request;
+
+typedef struct {
+  double wall_s, gpix_s;
+  double p50_ms, p99_ms, mean_ms, max_ms; /* latency: arrival -> done */
+  int64_t requests, pixels, batches;
+  double mean_batch;
+  int64_t peak_arena_bytes;
+  int32_t max_inflight;
+  int32_t errors;
+} fs_serve_stats;
+
+typedef struct fs_server fs_server;
+int fs_server_new(fs_ctx *ctx, fs_server **out, const fs_map *const *maps, int32_t nmaps,
+                  const fs_params *params, const fs_server_config *cfg);
+void fs_server_free(fs_server *srv);
+/* Runs the request loop until every request completes. realtime = 1 releases
+ * each request at its arrival_ns (the loop paces itself on the host clock);
+ * realtime = 0 releases all at once. Requests need not be sorted. */
+int fs_server_run(fs_server *srv, fs_request *reqs, int32_t n, int32_t realtime,
+                  fs_serve_stats *stats);
 
 /* ---- synthetic inputs (seeded, identical on every host) -------------------- */
 /* Toroidal diamond-square height map, rescaled to 0..255. size must be a power
