@@ -147,6 +147,19 @@ int fs_render_device(fs_ctx *ctx, const fs_map *map, const fs_camera *cam,
 /* Same into HOST memory `out_host`: renders, copies the frame back and waits. */
 int fs_render(fs_ctx *ctx, const fs_map *map, const fs_camera *cam, const fs_params *params,
               int32_t width, int32_t height, uint32_t *out_host);
+/* Allocation-free variant of fs_render_device (no counterpart in the
+ * reference). For callers that cannot let a library call cudaMalloc -- hosts
+ * that own all device memory through their own pool, or per-frame loops that
+ * cannot take the device synchronisation an allocation may cause: it calls no
+ * allocating routine. Its one scratch buffer, the per-depth view-line table, is
+ * a fixed 1.25 MiB array compiled into the library (held on every GPU that
+ * loads the library until exit), so a frame may use at most 65536 depth
+ * samples; longer schedules fail with FS_ERR_ARG. All calls share that array:
+ * calls that overlap on the GPU race. The first call on a device looks up the
+ * array's address (one-time set-up); make it before any stream capture. */
+int fs_render_device_noalloc(fs_ctx *ctx, const fs_map *map, const fs_camera *cam,
+                             const fs_params *params, int32_t width, int32_t height,
+                             uint32_t *out_dev);
 
 /* ---- batched multi-view render -------------------------------------------
  * A plan fixes the views' screen sizes and draw distances, owns a device
