@@ -53,7 +53,25 @@ def walk_views(fs, hm, seed: int):
                                                   screen_h=1080)]
 
 
+# the large-map workload's fused epilogue: depth shading + fog (not in the reference)
+LARGE_FX = dict(effects=3, shade=0.5, fog_start=1500.0, fog_end=6000.0, fog_color=0xFFA0B0C0)
+
+
+def workload_params(fs, name: str):
+    return fs.default_params(**LARGE_FX) if name == "large4k" else fs.default_params()
+
+
 def make_workload(fs, name: str, rank: int):
+    if name == "large4k":
+        hm = fs.gen_heights(MAP_SEED_H + 100, 16384, 0.6)
+        cm = fs.gen_colors(MAP_SEED_C + 100, hm, 12)
+        cams = fs.gen_cameras(VIEW_SEED + 17 + rank, hm, 32, above=(30.0, 150.0),
+                              distance=(6000.0, 6000.0), screen_h=2160)
+        return hm, cm, [(c, 3840, 2160) for c in cams], {
+            "workload": "large4k: 32 views 3840x2160, D=6000, 16384^2 maps (roughness 0.6), "
+                        "depth shading + fog epilogue",
+            "views": 32, "map": "16384x16384 u8 heights + u32 colours (beyond L2)",
+            "effects": LARGE_FX}
     if name == "batch512":
         hm = fs.gen_heights(MAP_SEED_H, 4096, 0.55)
         cm = fs.gen_colors(MAP_SEED_C, hm, 12)
@@ -154,10 +172,10 @@ def profiled_traffic(name: str):
     return None
 
 
-def cpu_reference_rate(views, hm, cm, max_seconds: float, threads: int):
+def cpu_reference_rate(views, hm, cm, max_seconds: float, threads: int, params=None):
     """Oracle (CPU restatement) Gpix/s on a bounded prefix of the views."""
     import oracle
-    params = oracle.make_params()
+    params = params or oracle.make_params()
     px = 0
     t0 = time.perf_counter()
     used = 0
@@ -177,6 +195,7 @@ def run_reference(args, rank: int, world: int):
     import futspace_gb300 as fs
     import oracle
     hm, cm, views, cfg = make_workload(fs, args.workload, 0)
+    oparams = oracle.params_from(workload_params(fs, args.workload))
     threads = oracle.lib().fso_max_threads()
     rates, pxs, dts = [], 0, 0.0
     order = list(range(len(views)))
@@ -184,7 +203,7 @@ def run_reference(args, rank: int, world: int):
         # each step: a bounded sample of the workload (views in a rotating order)
         k = (step * 7) % len(views)
         sample = [views[(k + i) % len(views)] for i in range(args.ref_views)]
-        g, used, px, dt = cpu_reference_rate(sample, hm, cm, args.ref_seconds, threads)
+        g, used, px, dt = cpu_reference_rate(sample, hm, cm, args.ref_seconds, threads, oparams)
         if step >= args.warmup:
             rates.append(g)
             pxs += px
@@ -293,7 +312,8 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="batch512", choices=["batch512", "walk1080", "serve"])
+    ap.add_argument("--workload", default="batch512",
+                    choices=["batch512", "walk1080", "large4k", "serve"])
     ap.add_argument("--serve-rates", default="1000,5000,10000,20000")
     ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--no-autotune", action="store_true")
@@ -331,7 +351,8 @@ def main():
     stream = torch.cuda.ExternalStream(ctx.stream_handle, device=local)
     hm, cm, views, cfg = make_workload(fs, args.workload, rank)
     fmap = fs.Map(ctx, hm, cm)
-    plan = fs.Plan(ctx, [fmap], views)
+    wparams = workload_params(fs, args.workload)
+    plan = fs.Plan(ctx, [fmap], views, params=wparams)
     tune_info = None
     if args.tune:
         plan.set_tune(*[int(x) for x in args.tune.split(",")])
@@ -388,7 +409,7 @@ def main():
         for cam, w, h in views:
             if (w, h) not in seen:
                 seen.add((w, h))
-                ctx.autotune_frame(fmap, cam, w, h, reps=3)
+                ctx.autotune_frame(fmap, cam, w, h, params=wparams, reps=3)
         plan.run_per_view()
         ctx.sync()
         t_plain = timed(plan.run_per_view, max(3, args.steps // 2))
@@ -433,7 +454,8 @@ def main():
     if rank == 0 and args.cpu_seconds > 0:
         import oracle
         threads = oracle.lib().fso_max_threads()
-        g, used, cpx, dt = cpu_reference_rate(views, hm, cm, args.cpu_seconds, threads)
+        g, used, cpx, dt = cpu_reference_rate(views, hm, cm, args.cpu_seconds, threads,
+                                              oracle.params_from(wparams))
         cpu = {"value": g, "unit": "Gpix/s", "cores": threads, "kind": "port",
                "sample": f"first {used} views of the workload ({cpx} px, {dt:.1f} s), CPU oracle "
                          "(C restatement of the reference render, OpenMP over columns)"}

@@ -28,6 +28,7 @@ __all__ = [
 
 NEAREST, BILINEAR = 0, 1
 GAP_ZERO, GAP_SKY = 0, 1
+FX_SHADE, FX_FOG = 1, 2
 _ERRORS = {1: "FS_ERR_ARG", 2: "FS_ERR_CUDA", 3: "FS_ERR_RANGE", 4: "FS_ERR_NOMEM",
            5: "FS_ERR_BUDGET", 6: "FS_ERR_STATE"}
 
@@ -52,7 +53,8 @@ class Params(C.Structure):
     _fields_ = [("invz_param1", C.c_float), ("invz_param2", C.c_float),
                 ("magic_number", C.c_float), ("height_filter", C.c_int32),
                 ("color_filter", C.c_int32), ("gap_rule", C.c_int32), ("floor_n", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("effects", C.c_int32), ("shade", C.c_float), ("fog_start", C.c_float),
+                ("fog_end", C.c_float), ("fog_color", C.c_uint32), ("smoothing", C.c_int32)]
 
 
 class Request(C.Structure):

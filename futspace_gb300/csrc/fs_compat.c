@@ -534,11 +534,9 @@ int futhark_entry_render(struct futhark_context *ctx, struct futhark_u32_2d **ou
   if (in->mode == MODE_MATH)
     return fs_fail(ctx->fs, FS_ERR_STATE,
                    "render: math mode (fut/interactive.fut:175-178) is not provided");
-  if (in->smoothing)
-    return fs_fail(ctx->fs, FS_ERR_STATE,
-                   "render: smoothing #on (fut/voxel_renderer.fut:175-213) is not provided");
   const int32_t H = in->height, W = in->width;
   fs_params p = fs_params_default();
+  p.smoothing = in->smoothing; /* key 2 toggles `#on` (fut/interactive.fut:120-125) */
   FsView v;
   int rc = fs_make_view(ctx->fs, &in->cam, &p, W, H, 0, &v);
   if (rc) return rc;

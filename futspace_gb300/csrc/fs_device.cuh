@@ -122,6 +122,25 @@ __device__ __forceinline__ uint32_t mix(const Channels &ch, float w1, uint32_t c
   return (to_byte(a) << 24) | (to_byte(r) << 16) | (to_byte(g) << 8) | to_byte(b);
 }
 
+/* matte colourspace.scale: RGB times s, alpha kept, then from_rgba. */
+__device__ __forceinline__ uint32_t scale(const Channels &ch, uint32_t c, float s) {
+  return (to_byte(ch(c, 24)) << 24) | (to_byte(fm(ch(c, 16), s)) << 16) |
+         (to_byte(fm(ch(c, 8), s)) << 8) | to_byte(fm(ch(c, 0), s));
+}
+
+/* The optional shading / fog epilogue of one sample at depth z (FSV_SHADE,
+ * FSV_FOG); not part of the reference's path. */
+__device__ __forceinline__ uint32_t apply_effects(const Channels &ch, const FsView &V,
+                                                  uint32_t c, float z) {
+  if (V.flags & FSV_SHADE) c = scale(ch, c, fs(1.0f, fm(V.shade, fd(z, V.distance))));
+  if (V.flags & FSV_FOG) {
+    float f = fd(fs(z, V.fog_start), fs(V.fog_end, V.fog_start));
+    f = (f < 0.0f) ? 0.0f : ((f > 1.0f) ? 1.0f : f);
+    c = mix(ch, fs(1.0f, f), c, f, V.fog_color);
+  }
+  return c;
+}
+
 /* png_color_filtered, fut/render_functions.fut:95-105 */
 __device__ __forceinline__ uint32_t color_bilinear(const FsMapDev &M, const Channels &ch,
                                                    float x, float y) {

@@ -85,6 +85,14 @@ int fs_check_params(fs_ctx *ctx, const fs_params *p) {
     return fs_fail(ctx, FS_ERR_ARG, "filter must be FS_NEAREST or FS_BILINEAR");
   if (p->gap_rule != FS_GAP_ZERO && p->gap_rule != FS_GAP_SKY)
     return fs_fail(ctx, FS_ERR_ARG, "gap_rule must be FS_GAP_ZERO or FS_GAP_SKY");
+  if (p->effects & ~(FS_FX_SHADE | FS_FX_FOG))
+    return fs_fail(ctx, FS_ERR_ARG, "unknown effect flags 0x%x", p->effects);
+  if ((p->effects & FS_FX_FOG) && !(p->fog_end > p->fog_start))
+    return fs_fail(ctx, FS_ERR_ARG, "fog needs fog_end > fog_start");
+  if (p->smoothing != 0 && p->smoothing != 1)
+    return fs_fail(ctx, FS_ERR_ARG, "smoothing must be 0 or 1");
+  if (p->smoothing && p->gap_rule != FS_GAP_ZERO)
+    return fs_fail(ctx, FS_ERR_ARG, "smoothing renders the live branch: gap_rule FS_GAP_ZERO");
   return FS_OK;
 }
 
@@ -123,7 +131,14 @@ int fs_make_view(fs_ctx *ctx, const fs_camera *cam, const fs_params *p, int32_t 
   v->gap = p->gap_rule == FS_GAP_SKY ? cam->sky_color : 0u;
   v->tmap = -1;
   v->flags = (p->height_filter == FS_BILINEAR ? FSV_HEIGHT_BILINEAR : 0) |
-             (p->color_filter == FS_BILINEAR ? FSV_COLOR_BILINEAR : 0);
+             (p->color_filter == FS_BILINEAR ? FSV_COLOR_BILINEAR : 0) |
+             ((p->effects & FS_FX_SHADE) ? FSV_SHADE : 0) | ((p->effects & FS_FX_FOG) ? FSV_FOG : 0) |
+             (p->smoothing ? FSV_SMOOTH : 0);
+  v->distance = cam->distance;
+  v->shade = p->shade;
+  v->fog_start = p->fog_start;
+  v->fog_end = p->fog_end;
+  v->fog_color = p->fog_color;
   return FS_OK;
 }
 
@@ -493,6 +508,11 @@ int fs_render_view(fs_ctx *ctx, const FsMapDev *map, FsView *v, const FsTune *tu
   else if (ctx->forced.tw) t = ctx->forced;
   else if (!fs_tune_lookup(ctx, v->W, v->H, map->MH, map->MW, v->flags, &t))
     t = fs_default_tune(ctx, stride);
+  t.smooth = (v->flags & FSV_SMOOTH) ? 1 : 0;
+  if (t.smooth && !fsk_tune_supported(&t)) {
+    const FsTune sm = {64, 1, 4, 0, 0, 1}; /* smoothing kernels: one lane per column */
+    t = sm;
+  }
   if (!t.tw || !fs_tune_fits(ctx, &t, stride))
     return fs_fail(ctx, FS_ERR_ARG, "no kernel configuration fits screen height %d", v->H);
   FsLaunch launch;

@@ -25,11 +25,14 @@ extern "C" {
 /* Levels of the height max pyramid (2^16 texels per side). */
 #define FS_PYR_MAX 16
 
-/* Filter flags of a view. */
+/* Flags of a view. */
 #define FSV_HEIGHT_BILINEAR 1
 #define FSV_COLOR_BILINEAR 2
+#define FSV_SHADE 4 /* FS_FX_SHADE epilogue */
+#define FSV_FOG 8   /* FS_FX_FOG epilogue */
+#define FSV_SMOOTH 16 /* `#on` smoothing */
 
-/* One view (camera + screen) as the kernels read it. 96 bytes. */
+/* One view (camera + screen) as the kernels read it. 128 bytes. */
 typedef struct {
   float cam_x, cam_y, cam_h, horizon;
   float sa, ca, fov, scale; /* sin/cos of the yaw from the host C library */
@@ -41,7 +44,10 @@ typedef struct {
   int64_t zoff;     /* first z-table entry of this view */
   int32_t tmap;     /* index into the tensor-map array, -1: plain stores */
   int32_t flags;    /* FSV_* */
-  int32_t pad[2];
+  float distance;   /* draw distance D (depth shading) */
+  float shade, fog_start, fog_end;
+  uint32_t fog_color;
+  int32_t pad[5];
 } FsView;
 
 /* One height/colour map pair resident in device memory. Heights are stored as
@@ -89,6 +95,7 @@ typedef struct {
   int32_t u;     /* depth samples per lane per chunk: chunk = lc * u depths */
   int32_t stage; /* 1: shared-memory column stage + TMA store; 0: direct painting */
   int32_t ctas;  /* persistent CTAs (0: as many as fit) */
+  int32_t smooth; /* 1: the `#on` smoothing kernels (FS_TUNE_LIST_SM) */
 } FsTune;
 
 /* Kernel-side entry points (fs_kernels.cu). Each returns a cudaError_t. */

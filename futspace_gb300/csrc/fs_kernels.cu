@@ -146,9 +146,13 @@ extern "C" int fsk_serve_prepare(const FsView *packed_dev, const int32_t *ids_de
 
 extern "C" int fsk_tune_supported(const FsTune *t) {
 #define FS_CASE(TW_, LC_, U_, STG_) \
-  if (t->tw == TW_ && t->lc == LC_ && t->u == U_ && t->stage == STG_) return 1;
+  if (t->tw == TW_ && t->lc == LC_ && t->u == U_ && t->stage == STG_ && !t->smooth) return 1;
+#define FS_CASE_SMOOTH(TW_, LC_, U_, STG_) \
+  if (t->tw == TW_ && t->lc == LC_ && t->u == U_ && t->stage == STG_ && t->smooth) return 1;
   FS_TUNE_LIST(FS_CASE)
+  FS_TUNE_LIST_SM(FS_CASE_SMOOTH)
 #undef FS_CASE
+#undef FS_CASE_SMOOTH
   return 0;
 }
 
@@ -157,7 +161,8 @@ extern "C" size_t fsk_render_smem(const FsTune *t, int32_t stride_max) {
   const size_t nw = (size_t)t->tw * t->lc / 32;
   const size_t box = t->stage ? 2ull * kBoxRows * t->tw * 4 : 0;
   const size_t stage = t->stage ? (size_t)t->tw * stride_max * 4 : 0;
-  return box + nw * queue_cap(t->u) * 8 + 256 * 4 + (size_t)t->tw * 8 + stage;
+  return box + nw * queue_cap(t->u) * 8 * (t->smooth ? 2 : 1) + 256 * 4 + (size_t)t->tw * 8 +
+         stage;
 }
 
 /* Level 1 of the max pyramid: each cell is the maximum of the 2x2 texels that

@@ -261,6 +261,10 @@ int fs_plan_new(fs_ctx *ctx, fs_plan **out, const fs_map *const *maps, int32_t n
     fs_plan_free(p);
     return fs_fail(ctx, FS_ERR_ARG, "no kernel configuration fits screen height %d", hmax);
   }
+  if (params->smoothing) {
+    const FsTune sm = {128, 1, 4, 0, 0, 1}; /* smoothing kernels: one lane per column */
+    t = sm;
+  }
   p->tune = t;
   rc = plan_build(p);
   if (rc) {
@@ -361,7 +365,7 @@ int fs_plan_get_tune(const fs_plan *p, int32_t out5[5]) {
 
 int fs_plan_set_tune(fs_plan *p, const int32_t tune5[5]) {
   if (!p || !tune5) return FS_ERR_ARG;
-  FsTune t = {tune5[0], tune5[1], tune5[2], tune5[3], tune5[4]};
+  FsTune t = {tune5[0], tune5[1], tune5[2], tune5[3], tune5[4], p->params.smoothing ? 1 : 0};
   if (!fs_tune_fits(p->ctx, &t, p->stride_max))
     return fs_fail(p->ctx, FS_ERR_ARG, "tuning (%d,%d,%d,%d) unsupported or too large", t.tw,
                    t.lc, t.u, t.stage);

@@ -102,14 +102,15 @@ __device__ __forceinline__ void fill_column(At at, int y_begin, int H, int mf, u
   }
 }
 
-template <int TW, int LC, int U, int STG>
+template <int TW, int LC, int U, int STG, int SM = 0>
 struct RenderShape {
   static constexpr int NT = TW * LC;
   static constexpr int NW = NT / 32;
   static constexpr int CPW = 32 / LC;
   static constexpr int QCAP = QueueCap<U>::value;
+  static constexpr int QW = SM ? 2 : 1; /* 8-byte words per queue entry */
   static constexpr size_t box_bytes = STG ? 2ull * kBoxRows * TW * 4 : 0;
-  static constexpr size_t queue_bytes = (size_t)NW * QCAP * 8;
+  static constexpr size_t queue_bytes = (size_t)NW * QCAP * 8 * QW;
   static constexpr size_t lut_bytes = 256 * 4;
   static constexpr size_t meta_bytes = (size_t)TW * 8;
   static constexpr size_t fixed_bytes = box_bytes + queue_bytes + lut_bytes + meta_bytes;
@@ -118,15 +119,26 @@ struct RenderShape {
   static constexpr int min_blocks = STG ? 1 : (NT >= 1024 ? 1 : 1024 / NT);
 };
 
-template <int TW, int LC, int U, int HF, int CF, int STG>
-__global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG>::min_blocks))
+/* SM = 1: the `#on` smoothing branch (fut/voxel_renderer.fut:175-213). Its
+ * scatter writes, at every prefix-minimum row, the tuple of the LAST sample
+ * holding that minimum (a sequential scatter: later writes win), so an event's
+ * rows blend with the previous event's colour only when the event held the
+ * minimum for a single sample (the next sample is an event too, or it is the
+ * last sample) and the previous event is the sample just before it (or there
+ * is none and the event is sample 1). The blend of row y in [row, prev) is
+ * mix(|row - y| / range, previous colour, |y - prev| / range, colour) with
+ * range = max(1, prev - row); colour 0 becomes sky, with no gap fill.
+ * Compiled for one lane per column and direct painting only. */
+template <int TW, int LC, int U, int HF, int CF, int STG, int SM = 0>
+__global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_blocks))
     render_kernel(const __grid_constant__ FsLaunch P) {
-  using S = RenderShape<TW, LC, U, STG>;
+  using S = RenderShape<TW, LC, U, STG, SM>;
   constexpr int NT = S::NT;
   constexpr int CPW = S::CPW;
   constexpr int CH = LC * U;
   constexpr int QCAP = S::QCAP;
   static_assert(NT % 32 == 0 && 32 % LC == 0 && TW % 4 == 0 && TW <= 128, "shape");
+  static_assert(!SM || (LC == 1 && STG == 0), "smoothing: one lane per column, direct paint");
 
   extern __shared__ __align__(1024) unsigned char smem[];
   uint32_t *box = reinterpret_cast<uint32_t *>(smem);
@@ -140,7 +152,7 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG>::min_bloc
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int dl = lane % LC;
   const int cl = warp * CPW + lane / LC;
-  unsigned long long *q = queues + warp * QCAP;
+  unsigned long long *q = queues + warp * QCAP * S::QW;
   unsigned lanemask_lt;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lanemask_lt));
   for (int i = tid; i < 256; i += NT) lut[i] = __fdiv_rn((float)i, 255.0f);
@@ -182,21 +194,54 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG>::min_bloc
 
     int m = H;          /* running minimum row of this column */
     int qh = 0, qt = 0; /* ring head / tail, warp-uniform */
+    /* smoothing: the last event of this lane's column, queued once the sample
+     * after it shows whether it held the minimum for a single sample */
+    int pend_k = -1, pend_r = 0, pend_p = 0, pend_kprev = -1;
+
+    /* colour of depth sample k of tile column ecl (with the optional epilogue) */
+    auto sample_colour = [&](int k, int ecl) -> uint32_t {
+      const float ec = (float)(c0 + ecl);
+      const float4 L = __ldg(zl + k);
+      const float x = fa(L.x, fm(ec, L.z));
+      const float y = fa(L.y, fm(ec, L.w));
+      uint32_t colour = CF ? color_bilinear(M, chan, x, y) : color_nearest(M, x, y);
+      if (Vp->flags & (FSV_SHADE | FSV_FOG)) {
+        /* depth of sample k, as the depth table computes it */
+        const float fi = (float)(k + 1);
+        const float z = fm(fd(fi, 2.0f), fa(fm(2.0f, Vp->z0), fm(fs(fi, 1.0f), Vp->d)));
+        colour = apply_effects(chan, *Vp, colour, z);
+      }
+      return colour;
+    };
 
     /* colour the queued events [qh, qh+cnt) and paint their intervals */
     auto drain = [&](int cnt) {
       if (lane < cnt) {
-        const unsigned long long e = q[(qh + lane) & (QCAP - 1)];
+        const int slot = (qh + lane) & (QCAP - 1);
+        const unsigned long long e = q[slot * S::QW];
         const int k = (int)(e >> 39);
         const int ecl = (int)((e >> 32) & 127u);
         const int er = (int)((e >> 16) & 0xFFFFu);
         const int ep = (int)(e & 0xFFFFu);
-        const float ec = (float)(c0 + ecl);
-        const float4 L = __ldg(zl + k);
-        const float x = fa(L.x, fm(ec, L.z));
-        const float y = fa(L.y, fm(ec, L.w));
-        const uint32_t colour = CF ? color_bilinear(M, chan, x, y) : color_nearest(M, x, y);
-        if (STG) {
+        const uint32_t colour = sample_colour(k, ecl);
+        if (SM) {
+          const unsigned long long e1 = q[slot * S::QW + S::QW - 1];
+          const int kprev = (int)(e1 & 0x1FFFFFu) - 1; /* previous event, -1: none */
+          const bool blend = ((e1 >> 32) & 1u) != 0;
+          uint32_t cprev = 0u;                         /* the scan's neutral colour */
+          if (blend && kprev >= 0) cprev = sample_colour(kprev, ecl);
+          const float range = fmaxf(1.0f, (float)(ep - er));
+          uint32_t *o = out + (size_t)er * W + c0 + ecl;
+          for (int yy = er; yy < ep; yy++, o += W) {
+            uint32_t c = colour;
+            if (blend) {
+              const float d1 = fd(fabsf(fs((float)yy, (float)ep)), range);
+              const float d2 = fd(fabsf(fs((float)er, (float)yy)), range);
+              c = mix(chan, d2, cprev, d1, colour);
+            }
+            __stcs(o, c == 0u ? sky : c);
+          }
+        } else if (STG) {
           uint32_t *sc = stage + ecl * stride;
           for (int yy = er; yy < ep; yy++) sc[yy] = colour;
         } else {
@@ -254,9 +299,30 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG>::min_bloc
 #pragma unroll
         for (int u = 0; u < U; u++) {
           const bool ev = r[u] < m;
-          const unsigned msk = __ballot_sync(FS_FULL_MASK, ev);
-          if (ev) q[(qt + __popc(msk & lanemask_lt)) & (QCAP - 1)] = pack_event(k0 + u, cl, r[u], m);
-          qt += __popc(msk);
+          if constexpr (SM) {
+            const int k = k0 + u;
+            const bool fin = ev && pend_k >= 0;
+            const unsigned msk = __ballot_sync(FS_FULL_MASK, fin);
+            if (fin) {
+              const int pos = (qt + __popc(msk & lanemask_lt)) & (QCAP - 1);
+              const bool blend = (k == pend_k + 1) &&
+                                 (pend_kprev == pend_k - 1 || (pend_kprev < 0 && pend_k == 1));
+              q[pos * S::QW] = pack_event(pend_k, cl, pend_r, pend_p);
+              q[pos * S::QW + S::QW - 1] =
+                  (unsigned long long)(uint32_t)(pend_kprev + 1) | ((unsigned long long)blend << 32);
+            }
+            qt += __popc(msk);
+            if (ev) {
+              pend_kprev = pend_k;
+              pend_k = k;
+              pend_r = r[u];
+              pend_p = m;
+            }
+          } else {
+            const unsigned msk = __ballot_sync(FS_FULL_MASK, ev);
+            if (ev) q[(qt + __popc(msk & lanemask_lt)) & (QCAP - 1)] = pack_event(k0 + u, cl, r[u], m);
+            qt += __popc(msk);
+          }
           m = min(m, r[u]);
         }
       } else {
@@ -295,6 +361,26 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG>::min_bloc
           m = min(m, __shfl_sync(FS_FULL_MASK, incl, LC - 1, LC));
         }
       }
+      __syncwarp();
+      while (qt - qh >= 32) {
+        drain(32);
+        qh += 32;
+      }
+    }
+    if constexpr (SM) {
+      /* the column's last event: no later sample is an event, so it held the
+       * minimum for a single sample only if it is the last sample */
+      const bool fin = pend_k >= 0;
+      const unsigned msk = __ballot_sync(FS_FULL_MASK, fin);
+      if (fin) {
+        const int pos = (qt + __popc(msk & lanemask_lt)) & (QCAP - 1);
+        const bool blend = (pend_k == n - 1) &&
+                           (pend_kprev == pend_k - 1 || (pend_kprev < 0 && pend_k == 1));
+        q[pos * S::QW] = pack_event(pend_k, cl, pend_r, pend_p);
+        q[pos * S::QW + S::QW - 1] =
+            (unsigned long long)(uint32_t)(pend_kprev + 1) | ((unsigned long long)blend << 32);
+      }
+      qt += __popc(msk);
       __syncwarp();
       while (qt - qh >= 32) {
         drain(32);
@@ -378,6 +464,12 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG>::min_bloc
 }
 
 }  // namespace fsd
+
+/* Configurations compiled with the `#on` smoothing branch (one lane per column,
+ * direct painting), for every filter pair. */
+#define FS_TUNE_LIST_SM(X) \
+  X(64, 1, 4, 0)           \
+  X(128, 1, 4, 0)
 
 /* The tuning table: (TW, LC, U, STG) compiled for every filter pair. */
 #define FS_TUNE_LIST(X) \

@@ -14,10 +14,12 @@ extern "C" int FS_RENDER_ENTRY(int op, const FsLaunch *L, const FsTune *t, int g
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return (int)e;
   if (dev < 0 || dev >= 64) return (int)cudaErrorInvalidDevice;
-#define FS_CASE(TW_, LC_, U_, STG_)                                                        \
-  if (t->tw == TW_ && t->lc == LC_ && t->u == U_ && t->stage == STG_) {                    \
+#define FS_CASE(TW_, LC_, U_, STG_) FS_CASE_SM(TW_, LC_, U_, STG_, 0)
+#define FS_CASE_SMOOTH(TW_, LC_, U_, STG_) FS_CASE_SM(TW_, LC_, U_, STG_, 1)
+#define FS_CASE_SM(TW_, LC_, U_, STG_, SM_)                                                 \
+  if (t->tw == TW_ && t->lc == LC_ && t->u == U_ && t->stage == STG_ && t->smooth == SM_) { \
     static int smem_set[64];                                                               \
-    auto kern = fsd::render_kernel<TW_, LC_, U_, FS_HF, FS_CF, STG_>;                      \
+    auto kern = fsd::render_kernel<TW_, LC_, U_, FS_HF, FS_CF, STG_, SM_>;                 \
     if (smem_set[dev] < (int)smem) {                                                       \
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
       if (e != cudaSuccess) return (int)e;                                                 \
@@ -29,6 +31,9 @@ extern "C" int FS_RENDER_ENTRY(int op, const FsLaunch *L, const FsTune *t, int g
     return (int)cudaGetLastError();                                                        \
   }
   FS_TUNE_LIST(FS_CASE)
+  FS_TUNE_LIST_SM(FS_CASE_SMOOTH)
 #undef FS_CASE
+#undef FS_CASE_SMOOTH
+#undef FS_CASE_SM
   return (int)cudaErrorInvalidValue;
 }

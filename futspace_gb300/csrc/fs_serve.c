@@ -203,6 +203,11 @@ int fs_server_new(fs_ctx *ctx, fs_server **out, const fs_map *const *maps, int32
     FsTune def = {128, 1, 4, 0, 0};
     t = def;
   }
+  if (params->smoothing) {
+    const FsTune sm = {128, 1, 4, 0, 0, 1};
+    if (!cfg->tune[0]) t = sm;
+    t.smooth = 1;
+  }
   if (t.stage != 0 || !fsk_tune_supported(&t)) {
     fs_server_free(s);
     return fs_fail(ctx, FS_ERR_ARG, "serving needs a compiled direct-paint configuration");

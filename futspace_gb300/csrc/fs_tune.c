@@ -151,7 +151,7 @@ int fs_autotune_frame(fs_ctx *ctx, const fs_map *map, const fs_camera *cam,
   for (int i = 0; i < fs_tune_count(); i++) {
     int32_t t5[5];
     fs_tune_get(i, t5);
-    FsTune t = {t5[0], t5[1], t5[2], t5[3], 0};
+    FsTune t = {t5[0], t5[1], t5[2], t5[3], 0, (j.view.flags & FSV_SMOOTH) ? 1 : 0};
     if (!fs_tune_fits(ctx, &t, height | 1)) continue;
     j.tune = t;
     float ms = 0.0f;
@@ -192,7 +192,7 @@ int fs_plan_autotune(fs_plan *p, int32_t reps, int32_t out5[5], float *best_ms) 
   for (int i = 0; i < fs_tune_count(); i++) {
     int32_t t5[5];
     fs_tune_get(i, t5);
-    FsTune t = {t5[0], t5[1], t5[2], t5[3], 0};
+    FsTune t = {t5[0], t5[1], t5[2], t5[3], 0, p->params.smoothing ? 1 : 0};
     if (!fs_tune_fits(ctx, &t, p->stride_max)) continue;
     rc = fs_plan_set_tune(p, t5);
     if (rc) break;
@@ -213,7 +213,7 @@ int fs_plan_autotune(fs_plan *p, int32_t reps, int32_t out5[5], float *best_ms) 
   char key[96];
   snprintf(key, sizeof(key), "batch:%016llx:map%dx%d:f%d", (unsigned long long)sig,
            p->maps[0].MH, p->maps[0].MW, p->hf | (p->cf << 1));
-  FsTune t = {bt[0], bt[1], bt[2], bt[3], 0};
+  FsTune t = {bt[0], bt[1], bt[2], bt[3], 0, 0};
   fs_tune_store(ctx, key, &t);
   memcpy(out5, bt, sizeof(bt));
   out5[4] = p->grid;

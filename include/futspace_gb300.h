@@ -41,6 +41,13 @@ typedef struct {
 
 enum { FS_NEAREST = 0, FS_BILINEAR = 1 };
 enum { FS_GAP_ZERO = 0, FS_GAP_SKY = 1 };
+/* Optional colour epilogue (not in the reference; 0 renders the reference's
+ * frames). Applied to every depth sample's colour before occlusion, in matte's
+ * colour arithmetic, with z the sample's depth and D the draw distance:
+ *   FS_FX_SHADE: c = scale(c, 1 - shade * (z / D))                 depth shading
+ *   FS_FX_FOG:   f = clamp((z - fog_start) / (fog_end - fog_start), 0, 1);
+ *                c = mix(1 - f, c, f, fog_color)                     distance fog */
+enum { FS_FX_SHADE = 1, FS_FX_FOG = 2 };
 
 /* Render parameters.
  *  invz_param1 : depth step d of the arithmetic depth series
@@ -57,8 +64,14 @@ enum { FS_GAP_ZERO = 0, FS_GAP_SKY = 1 };
  *  floor_n     : 1 floors the depth count before the i32 conversion
  *                (fut/voxel_renderer.fut:32); 0 converts directly
  *                (tests/futspace.fut:51). Identical for positive counts.
+ *  effects, shade, fog_start, fog_end, fog_color: the optional epilogue
+ *                above (FS_FX_* flags; fog needs fog_end > fog_start).
+ *  smoothing   : 1 renders the reference's `#on` smoothing branch
+ *                (fut/voxel_renderer.fut:175-213, key 2 of the interactive app):
+ *                rows between two consecutive new minima blend their colours;
+ *                colour 0 becomes sky. Requires FS_GAP_ZERO.
  * fs_params_default() gives the live reference path: 0.001, 0.0, w/2,
- * bilinear height and colour, FS_GAP_ZERO, floor_n 1. */
+ * bilinear height and colour, FS_GAP_ZERO, floor_n 1, no effects. */
 typedef struct {
   float invz_param1;
   float invz_param2;
@@ -67,7 +80,11 @@ typedef struct {
   int32_t color_filter;
   int32_t gap_rule;
   int32_t floor_n;
-  int32_t reserved;
+  int32_t effects;
+  float shade;
+  float fog_start, fog_end;
+  uint32_t fog_color;
+  int32_t smoothing;
 } fs_params;
 
 /* One view of a batch: a camera, a screen size and the map it samples. */

@@ -38,7 +38,9 @@ class OCamera(C.Structure):
 class OParams(C.Structure):
     _fields_ = [("d", C.c_float), ("z0", C.c_float), ("scale", C.c_float),
                 ("height_filter", C.c_int32), ("color_filter", C.c_int32),
-                ("gap_rule", C.c_int32), ("floor_n", C.c_int32), ("pad", C.c_int32)]
+                ("gap_rule", C.c_int32), ("floor_n", C.c_int32), ("effects", C.c_int32),
+                ("shade", C.c_float), ("fog_start", C.c_float), ("fog_end", C.c_float),
+                ("fog_color", C.c_uint32), ("smoothing", C.c_int32)]
 
 
 _LIB = None
@@ -94,14 +96,17 @@ def to_ocam(cam) -> OCamera:
 
 
 def make_params(d=0.001, z0=0.0, scale=0.0, height_filter=BILINEAR, color_filter=BILINEAR,
-                gap_rule=GAP_ZERO, floor_n=1) -> OParams:
-    return OParams(d, z0, scale, height_filter, color_filter, gap_rule, floor_n, 0)
+                gap_rule=GAP_ZERO, floor_n=1, effects=0, shade=0.0, fog_start=0.0, fog_end=0.0,
+                fog_color=0, smoothing=0) -> OParams:
+    return OParams(d, z0, scale, height_filter, color_filter, gap_rule, floor_n, effects, shade,
+                   fog_start, fog_end, fog_color, smoothing)
 
 
 def params_from(p) -> OParams:
     """From a futspace_gb300.Params."""
     return make_params(p.invz_param1, p.invz_param2, p.magic_number, p.height_filter,
-                       p.color_filter, p.gap_rule, p.floor_n)
+                       p.color_filter, p.gap_rule, p.floor_n, p.effects, p.shade, p.fog_start,
+                       p.fog_end, p.fog_color, getattr(p, "smoothing", 0))
 
 
 def render(cam, params: OParams, heights: np.ndarray, colors: np.ndarray, width: int,

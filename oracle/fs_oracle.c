@@ -152,6 +152,20 @@ uint32_t fso_color_nearest(const uint32_t *cm, int32_t MH, int32_t MW, float x, 
   return cm[(int64_t)iy * MW + ix];
 }
 
+/* ---- optional epilogue (not in the reference) ------------------------------
+ * Applied to a sample's colour at depth z with draw distance D, in matte's
+ * arithmetic: shade c = scale(c, 1 - shade * (z / D)); fog f = clamp((z -
+ * fog_start) / (fog_end - fog_start), 0, 1), c = mix(1 - f, c, f, fog). */
+static uint32_t fso_effects(const fso_params *p, uint32_t c, float z, float D) {
+  if (p->effects & 1) c = fso_scale(c, 1.0f - p->shade * (z / D));
+  if (p->effects & 2) {
+    float f = (z - p->fog_start) / (p->fog_end - p->fog_start);
+    f = (f < 0.0f) ? 0.0f : ((f > 1.0f) ? 1.0f : f);
+    c = fso_mix(1.0f - f, c, f, p->fog_color);
+  }
+  return c;
+}
+
 /* ---- render (fut/voxel_renderer.fut:101-251, `#off` branch) -------------- */
 
 typedef struct {
@@ -188,7 +202,7 @@ static int fso_check(const fso_params *p, const uint8_t *hm, const uint32_t *cm,
  * samplers, the projection `i32.max 0 (i32.f32 relative_height)`). */
 static void fso_sample(const fso_camera *cam, const fso_params *p, const uint8_t *hm,
                        int32_t MH, int32_t MW, const uint32_t *cm, int32_t CH, int32_t CW,
-                       const fso_line *l, float inv_z, int32_t i, uint32_t *colour,
+                       const fso_line *l, float z, float inv_z, int32_t i, uint32_t *colour,
                        int32_t *row) {
   float x = l->start_x + (float)i * l->end_x;
   float y = l->start_y + (float)i * l->end_y;
@@ -199,6 +213,7 @@ static void fso_sample(const fso_camera *cam, const fso_params *p, const uint8_t
   float height_diff = cam->height - mh;
   float relative_height = height_diff * inv_z + cam->horizon;
   int32_t r = fso_f2i(relative_height);
+  if (p->effects) c = fso_effects(p, c, z, cam->distance);
   *colour = c;
   *row = r > 0 ? r : 0;
 }
@@ -233,6 +248,60 @@ static void fso_column(const uint32_t *cs, const int32_t *rs, int32_t n, int32_t
   }
 }
 
+/* One screen column of the `#on` branch (fut/voxel_renderer.fut:175-213):
+ * scan occlude2 (:88-91) with neutral (0, h, 0) carrying the depth index; the
+ * tuples (colour, previous colour, row, previous row, index, previous index)
+ * with `rotate (-1)` (the previous element, wrapping to the last); scatter into
+ * rows, duplicates written in index order so the last write wins (a sequential
+ * `futhark c` scatter); forward fill of whole tuples against the empty tuple
+ * (0,0,0,0,1000,1000) (fill_vline3, :93-96); the per-row blend when the two
+ * indices are adjacent; 0 -> sky. */
+typedef struct {
+  uint32_t c, cp;
+  int32_t r, rp, i, ip;
+} fso_tuple;
+
+static int fso_tuple_empty(const fso_tuple *t) {
+  return t->c == 0 && t->cp == 0 && t->r == 0 && t->rp == 0 && t->i == 1000 && t->ip == 1000;
+}
+
+static void fso_column_smooth(const uint32_t *cs, const int32_t *rs, int32_t n, int32_t H,
+                              uint32_t sky, uint32_t *sc, int32_t *sr, int32_t *si,
+                              fso_tuple *line, uint32_t *vline) {
+  uint32_t acc_c = 0;
+  int32_t acc_r = H, acc_i = 0;
+  for (int32_t k = 0; k < n; k++) {
+    if (!(acc_r <= rs[k])) {
+      acc_c = cs[k];
+      acc_r = rs[k];
+      acc_i = k;
+    }
+    sc[k] = acc_c;
+    sr[k] = acc_r;
+    si[k] = acc_i;
+  }
+  const fso_tuple empty = {0, 0, 0, 0, 1000, 1000};
+  for (int32_t y = 0; y < H; y++) line[y] = empty;
+  for (int32_t k = 0; k < n; k++) {
+    const int32_t kp = (k == 0) ? n - 1 : k - 1;
+    const int32_t r = sr[k];
+    if (r >= 0 && r < H) {
+      fso_tuple t = {sc[k], sc[kp], sr[k], sr[kp], si[k], si[kp]};
+      line[r] = t;
+    }
+  }
+  fso_tuple fill = empty;
+  for (int32_t y = 0; y < H; y++) {
+    if (!fso_tuple_empty(&line[y])) fill = line[y];
+    const fso_tuple *t = &fill;
+    const float range = fmaxf(1.0f, (float)(t->rp - t->r));
+    const float delta1 = fabsf((float)y - (float)t->rp) / range;
+    const float delta2 = fabsf((float)t->r - (float)y) / range;
+    const uint32_t col = (t->i - t->ip == 1) ? fso_mix(delta2, t->cp, delta1, t->c) : t->c;
+    vline[y] = (col == 0) ? sky : col;
+  }
+}
+
 static int32_t fso_render_impl(const fso_camera *cam, const fso_params *p, const uint8_t *hm,
                                int32_t MH, int32_t MW, const uint32_t *cm, int32_t CH,
                                int32_t CW, int32_t W, int32_t H, uint32_t *out,
@@ -261,7 +330,7 @@ static int32_t fso_render_impl(const fso_camera *cam, const fso_params *p, const
     fso_line l = fso_get_h_line(zs[k], cam, W);
     float inv_z = (1.0f / zs[k]) * scale;
     for (int32_t i = 0; i < W; i++)
-      fso_sample(cam, p, hm, MH, MW, cm, CH, CW, &l, inv_z, i, &pc[(size_t)k * W + i],
+      fso_sample(cam, p, hm, MH, MW, cm, CH, CW, &l, zs[k], inv_z, i, &pc[(size_t)k * W + i],
                  &pr[(size_t)k * W + i]);
   }
 
@@ -273,7 +342,9 @@ static int32_t fso_render_impl(const fso_camera *cam, const fso_params *p, const
     uint32_t *ac = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)n);
     int32_t *ar = (int32_t *)malloc(sizeof(int32_t) * (size_t)n);
     uint32_t *vline = (uint32_t *)malloc(sizeof(uint32_t) * (size_t)H);
-    if (!cs || !rs || !ac || !ar || !vline) {
+    int32_t *ai = (int32_t *)malloc(sizeof(int32_t) * (size_t)n);
+    fso_tuple *line = (fso_tuple *)malloc(sizeof(fso_tuple) * (size_t)H);
+    if (!cs || !rs || !ac || !ar || !vline || !ai || !line) {
 #pragma omp atomic write
       failed = 1;
     } else {
@@ -283,7 +354,10 @@ static int32_t fso_render_impl(const fso_camera *cam, const fso_params *p, const
           cs[k] = pc[(size_t)k * W + i];
           rs[k] = pr[(size_t)k * W + i];
         }
-        fso_column(cs, rs, n, H, gap, cam->sky_color, ac, ar, vline);
+        if (p->smoothing)
+          fso_column_smooth(cs, rs, n, H, cam->sky_color, ac, ar, ai, line, vline);
+        else
+          fso_column(cs, rs, n, H, gap, cam->sky_color, ac, ar, vline);
         for (int32_t y = 0; y < H; y++) out[(size_t)y * W + i] = vline[y];
       }
     }
@@ -292,6 +366,8 @@ static int32_t fso_render_impl(const fso_camera *cam, const fso_params *p, const
     free(ac);
     free(ar);
     free(vline);
+    free(ai);
+    free(line);
   }
   free(zs);
   free(pc);

@@ -40,7 +40,11 @@ typedef struct {
   int32_t color_filter;
   int32_t gap_rule;
   int32_t floor_n;  /* 1: n = i32(floor(num/div)) (:32); 0: i32(num/div) (tests/futspace.fut:51) */
-  int32_t pad;
+  int32_t effects;  /* optional epilogue, not in the reference: 1 shade, 2 fog */
+  float shade;
+  float fog_start, fog_end;
+  uint32_t fog_color;
+  int32_t smoothing; /* 1: the `#on` branch, fut/voxel_renderer.fut:175-213 */
 } fso_params;
 
 int32_t  fso_f2i(float v);

@@ -80,8 +80,59 @@ def _gather(m, iy, ix):
     return m[np.mod(iy, m.shape[0]), np.mod(ix, m.shape[1])]
 
 
+def scale_colour(c, s):
+    """matte colourspace.scale (RGB times s, alpha kept)."""
+    r, g, b, a = _to_rgba(np.asarray(c))
+    s = np.asarray(s, np.float32)
+    return _from_rgba(r * s, g * s, b * s, a)
+
+
+def _smooth(col, row, n, W, H, sky):
+    """The `#on` branch, fut/voxel_renderer.fut:175-213, columns vectorised."""
+    acc_c = np.zeros(W, np.uint32)
+    acc_r = np.full(W, H, np.int64)
+    acc_i = np.zeros(W, np.int64)
+    sc = np.empty((n, W), np.uint32)
+    sr = np.empty((n, W), np.int64)
+    si = np.empty((n, W), np.int64)
+    for k in range(n):  # scan occlude2 with neutral (0, h, 0)
+        take = ~(acc_r <= row[k])
+        acc_c = np.where(take, col[k], acc_c)
+        acc_r = np.where(take, row[k], acc_r)
+        acc_i = np.where(take, k, acc_i)
+        sc[k], sr[k], si[k] = acc_c, acc_r, acc_i
+    # rotate (-1): element k pairs with element k-1 (element 0 with element n-1)
+    pc, pr, pi = np.roll(sc, 1, axis=0), np.roll(sr, 1, axis=0), np.roll(si, 1, axis=0)
+    fields = [np.zeros((H, W), np.uint32), np.zeros((H, W), np.uint32),
+              np.zeros((H, W), np.int64), np.zeros((H, W), np.int64),
+              np.full((H, W), 1000, np.int64), np.full((H, W), 1000, np.int64)]
+    cols = np.arange(W)
+    for k in range(n):  # scatter, later indices overwrite earlier ones
+        ok = sr[k] < H
+        rr, cc = sr[k][ok], cols[ok]
+        for f, v in zip(fields, (sc[k], pc[k], sr[k], pr[k], si[k], pi[k])):
+            f[rr, cc] = v[ok]
+    carry = [np.zeros(W, np.uint32), np.zeros(W, np.uint32), np.zeros(W, np.int64),
+             np.zeros(W, np.int64), np.full(W, 1000, np.int64), np.full(W, 1000, np.int64)]
+    out = np.empty((H, W), np.uint32)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        for y in range(H):
+            t = [f[y] for f in fields]
+            empty = ((t[0] == 0) & (t[1] == 0) & (t[2] == 0) & (t[3] == 0) & (t[4] == 1000)
+                     & (t[5] == 1000))
+            carry = [np.where(empty, c, v) for c, v in zip(carry, t)]
+            c0, c1, r2, r3, i4, i5 = carry
+            rng = np.maximum(f32(1), (r3 - r2).astype(np.float32))
+            d1 = np.abs(f32(y) - r3.astype(np.float32)) / rng
+            d2 = np.abs(r2.astype(np.float32) - f32(y)) / rng
+            c = np.where(i4 - i5 == 1, mix(d2, c1, d1, c0), c0).astype(np.uint32)
+            out[y] = np.where(c == 0, sky, c)
+    return out
+
+
 def render(cam, hm, cm, W, H, d=0.001, z0=0.0, scale=0.0, height_filter=1, color_filter=1,
-           gap_rule=0, floor_n=1) -> np.ndarray:
+           gap_rule=0, floor_n=1, effects=0, shade=0.0, fog_start=0.0, fog_end=0.0,
+           fog_color=0, smoothing=0) -> np.ndarray:
     """fut/voxel_renderer.fut:101-251 (`#off`) with the samplers of
     fut/render_functions.fut:63-105."""
     get = (lambda k: cam[k]) if isinstance(cam, dict) else (lambda k: getattr(cam, k))
@@ -126,7 +177,16 @@ def render(cam, hm, cm, W, H, d=0.001, z0=0.0, scale=0.0, height_filter=1, color
         else:
             col = _gather(cm, f2i(y), f2i(x)).astype(np.uint32)
         rel = (ch_ - mh) * inv_z[:, None] + hor
+        zz = np.broadcast_to(zs[:, None], col.shape).astype(np.float32)
+        if effects & 1:
+            col = scale_colour(col, f32(1) - f32(shade) * (zz / D))
+        if effects & 2:
+            fo = (zz - f32(fog_start)) / (f32(fog_end) - f32(fog_start))
+            fo = np.where(fo < f32(0), f32(0), np.where(fo > f32(1), f32(1), fo)).astype(np.float32)
+            col = mix(f32(1) - fo, col, fo, np.uint32(fog_color))
     row = np.maximum(0, f2i(rel))
+    if smoothing:
+        return _smooth(col, row, zs.size, W, H, np.uint32(sky))
     # per column: scan occlude with neutral (0, h) (:231), scatter (:244),
     # scan fill_vline (:246), sky (:248); columns vectorised
     n = zs.size

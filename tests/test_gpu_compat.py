@@ -180,11 +180,21 @@ def test_interactive_session(fs, orc):
         assert t[2] == f32(f32(2.2) + f32(0.10)) and t[4] == 220.0
         assert count_diff(app.render(), expected_frame(0.1, 0.1, sky2)) == 0
 
-        # smoothing #on is not provided: render reports an error instead of pixels
+        # key 2 toggles the `#on` smoothing branch
         app.apply(app.L.futhark_entry_key, 0, ord("2"))
         app.apply(app.L.futhark_entry_step, f32(0.016))
         app.apply(app.L.futhark_entry_key, 1, ord("2"))
-        with pytest.raises(AssertionError, match="smoothing"):
+        shadow = orc.shadowmap(hm, cm, sun_vector(0.1, 0.1), threads=0)
+        x, y, ang, height, hor, dist, _, _, fov = app.text()
+        cam = dict(x=x, y=y, height=height, angle=ang, horizon=hor, distance=dist, fov=fov,
+                   sky_color=sky2)
+        want = orc.render(cam, orc.make_params(smoothing=1), hm, shadow, 160, 120, threads=0)
+        assert count_diff(app.render(), want) == 0
+        # math mode (key 1) is not provided: render reports an error instead of pixels
+        app.apply(app.L.futhark_entry_key, 0, ord("1"))
+        app.apply(app.L.futhark_entry_step, f32(0.016))
+        app.apply(app.L.futhark_entry_key, 1, ord("1"))
+        with pytest.raises(AssertionError, match="math mode"):
             app.render()
     finally:
         app.close()

@@ -198,3 +198,66 @@ def test_chunk_skip_is_exact_and_saves_work(fs, orc, gpu_ctx):
         s_on, e_on = counts[(1, tune)]
         assert e_on == e_off          # the same occlusion events are coloured
         assert s_on < s_off           # fewer depth samples are evaluated
+
+
+@pytest.mark.parametrize("effects", [1, 2, 3])
+def test_effects_epilogue(fs, orc, gpu_ctx, maps1024, effects):
+    """Depth shading / fog fused into the colour path: bit-exact vs the oracle,
+    for single frames (every configuration) and a batch plan."""
+    hm, cm = maps1024
+    fmap = fs.Map(gpu_ctx, hm, cm)
+    p = fs.default_params(effects=effects, shade=0.5, fog_start=100.0, fog_end=900.0,
+                          fog_color=0xFFA0B0C0)
+    views = _mixed_views(fs, hm, 101 + effects, 6)
+    refs = [_oracle(orc, c, p, hm, cm, w, h) for c, w, h in views]
+    try:
+        for tune in fs.tune_table():
+            gpu_ctx.force_tune(tune)
+            for (c, w, h), r in zip(views[:2], refs[:2]):
+                assert count_diff(gpu_ctx.render(fmap, c, w, h, params=p), r) == 0, tune
+    finally:
+        gpu_ctx.force_tune(None)
+    plan = fs.Plan(gpu_ctx, [fmap], views, params=p)
+    plan.run()
+    assert all(count_diff(f, r) == 0 for f, r in zip(plan.frames(), refs))
+    with pytest.raises(fs.FsError):
+        gpu_ctx.render(fmap, views[0][0], 64, 48,
+                       params=fs.default_params(effects=2, fog_start=5.0, fog_end=5.0))
+
+
+def test_large_map_4k_with_effects(fs, orc, gpu_ctx):
+    """3840x2160 frames, D=6000 (n=3464), over a 16384^2 map (beyond L2), with the
+    depth shading + fog epilogue: bit-exact vs the oracle."""
+    hm = fs.gen_heights(107, 16384, 0.6)
+    cm = fs.gen_colors(108, hm, 12)
+    fmap = fs.Map(gpu_ctx, hm, cm)
+    p = fs.default_params(effects=3, shade=0.5, fog_start=1500.0, fog_end=6000.0,
+                          fog_color=0xFFA0B0C0)
+    cams = fs.gen_cameras(109, hm, 2, above=(30, 150), distance=(6000, 6000), screen_h=2160)
+    plan = fs.Plan(gpu_ctx, [fmap], [(c, 3840, 2160) for c in cams], params=p)
+    plan.run()
+    for c, f in zip(cams, plan.frames()):
+        assert count_diff(f, _oracle(orc, c, p, hm, cm, 3840, 2160)) == 0
+    fmap.close()
+
+
+@pytest.mark.parametrize("hf,cf", FILTERS)
+def test_smoothing_branch(fs, orc, gpu_ctx, maps256, hf, cf):
+    """`#on` smoothing: single frames, a batch plan and near-field cameras that
+    blend many rows; bit-exact vs the oracle."""
+    hm, cm = maps256
+    fmap = fs.Map(gpu_ctx, hm, cm)
+    p = fs.default_params(height_filter=hf, color_filter=cf, smoothing=1)
+    views = _mixed_views(fs, hm, 111 + hf + 2 * cf, 6)
+    near = fs.Camera(100.5, 80.25, float(hm[80, 100]) + 3.0, 0.7, 20.0, 60.0, 1.2, 0xFF9090E0)
+    views.append((near, 64, 40))
+    for c, w, h in views:
+        assert count_diff(gpu_ctx.render(fmap, c, w, h, params=p),
+                          _oracle(orc, c, p, hm, cm, w, h)) == 0
+    plan = fs.Plan(gpu_ctx, [fmap], views, params=p)
+    plan.run()
+    for (c, w, h), f in zip(views, plan.frames()):
+        assert count_diff(f, _oracle(orc, c, p, hm, cm, w, h)) == 0
+    with pytest.raises(fs.FsError):
+        gpu_ctx.render(fmap, views[0][0], 64, 48,
+                       params=fs.default_params(smoothing=1, gap_rule=1))

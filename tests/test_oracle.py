@@ -63,7 +63,9 @@ def _case(fs, orc, hm, cm, cam, W, H, **kw):
     a = orc.render(cam, p, hm, cm, W, H)
     b = literal.render(cam, hm, cm, W, H, d=p.d, z0=p.z0, scale=p.scale,
                        height_filter=p.height_filter, color_filter=p.color_filter,
-                       gap_rule=p.gap_rule, floor_n=p.floor_n)
+                       gap_rule=p.gap_rule, floor_n=p.floor_n, effects=p.effects, shade=p.shade,
+                       fog_start=p.fog_start, fog_end=p.fog_end, fog_color=p.fog_color,
+                       smoothing=p.smoothing)
     assert count_diff(a, b) == 0
     return a
 
@@ -158,3 +160,29 @@ def test_shadowmap_restatement(fs, orc):
                 count += 1
         want = literal.mix(f(4) * f(count), np.uint32(0xFF000000), f(1), cm[y % 256, x % 256])
         assert int(out[y, x]) == int(want)
+
+
+@pytest.mark.parametrize("effects", [1, 2, 3])
+def test_effects_restatements_agree(fs, orc, maps256, effects):
+    """The optional shading/fog epilogue (not part of the reference path)."""
+    hm, cm = maps256
+    for cam in fs.gen_cameras(91, hm, 3, above=(20, 90), distance=(200, 500), screen_h=40):
+        _case(fs, orc, hm, cm, cam, 56, 40, effects=effects, shade=0.6, fog_start=50.0,
+              fog_end=float(cam.distance) * 0.8, fog_color=0xFFB0B8C8)
+
+
+@pytest.mark.parametrize("hf,cf", [(1, 1), (0, 0), (1, 0)])
+def test_smoothing_restatements_agree(fs, orc, maps256, hf, cf):
+    """The `#on` smoothing branch (fut/voxel_renderer.fut:175-213)."""
+    hm, cm = maps256
+    for cam in fs.gen_cameras(93 + hf + 2 * cf, hm, 4, above=(10, 90), distance=(100, 400),
+                              screen_h=40):
+        on = _case(fs, orc, hm, cm, cam, 56, 40, height_filter=hf, color_filter=cf,
+                   smoothing=1)
+        assert on.shape == (40, 56)
+    # near-field cameras low over the terrain blend many rows
+    cam = dict(x=100.5, y=80.25, height=float(hm[80, 100]) + 3.0, angle=0.7, horizon=20.0,
+               distance=60.0, fov=1.2, sky_color=0xFF9090E0)
+    on = _case(fs, orc, hm, cm, cam, 64, 40, smoothing=1)
+    off = _case(fs, orc, hm, cm, cam, 64, 40)
+    assert count_diff(on, off) > 0
