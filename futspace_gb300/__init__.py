@@ -158,6 +158,7 @@ def lib():
     _sig(L, "fs_plan_set_cameras", C.c_int, [vp, P(Camera), i32])
     _sig(L, "fs_plan_run", C.c_int, [vp])
     _sig(L, "fs_plan_run_per_view", C.c_int, [vp])
+    _sig(L, "fs_plan_kernel_ms", C.c_int, [vp, P(f32)])
     _sig(L, "fs_plan_frame_dev", vp, [vp, i32])
     _sig(L, "fs_plan_frame_offset", i64, [vp, i32])
     _sig(L, "fs_plan_total_pixels", i64, [vp])
@@ -424,6 +425,12 @@ class Plan:
 
     def run_per_view(self):
         self.ctx.check(lib().fs_plan_run_per_view(self._h), "fs_plan_run_per_view")
+
+    def kernel_ms(self) -> float:
+        """Device time of the render kernel in the last run (waits for it)."""
+        ms = C.c_float()
+        self.ctx.check(lib().fs_plan_kernel_ms(self._h, C.byref(ms)), "fs_plan_kernel_ms")
+        return ms.value
 
     def set_cameras(self, cams: Iterable[Camera]):
         cams = list(cams)

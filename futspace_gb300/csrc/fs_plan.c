@@ -38,6 +38,8 @@ void fs_plan_free(fs_plan *p) {
   cudaSetDevice(p->ctx->device);
   cudaStreamSynchronize(p->ctx->stream);
   plan_release_graph(p);
+  for (int i = 0; i < 2; i++)
+    if (p->ev_render[i]) cudaEventDestroy(p->ev_render[i]);
   cudaFree(p->fv_d);
   cudaFree(p->tm_d);
   cudaFree(p->items_d);
@@ -81,8 +83,14 @@ static int plan_enqueue(fs_plan *p) {
   if (e) return fs_cuda_fail(ctx, e, "work counter reset");
   e = fsk_ztable(p->fv_d, NULL, p->nviews, max_n, p->zline, p->zinvz, ctx->stream);
   if (e) return fs_cuda_fail(ctx, e, "z-table kernel launch");
+  /* external event nodes bracket the render kernel, so its device time is
+   * readable after every replay of the graph */
+  e = cudaEventRecordWithFlags(p->ev_render[0], ctx->stream, cudaEventRecordExternal);
+  if (e) return fs_cuda_fail(ctx, e, "render start event");
   e = fsk_render(&launch, &p->tune, p->hf, p->cf, p->grid, ctx->stream);
   if (e) return fs_cuda_fail(ctx, e, "persistent render kernel launch");
+  e = cudaEventRecordWithFlags(p->ev_render[1], ctx->stream, cudaEventRecordExternal);
+  if (e) return fs_cuda_fail(ctx, e, "render end event");
   return FS_OK;
 }
 
@@ -145,6 +153,12 @@ static int plan_build(fs_plan *p) {
   if (grid > nitems) grid = nitems;
   p->grid = (int32_t)grid;
 
+  for (int i = 0; i < 2; i++) {
+    if (!p->ev_render[i]) {
+      e = cudaEventCreate(&p->ev_render[i]);
+      if (e) return fs_cuda_fail(ctx, e, "cudaEventCreate");
+    }
+  }
   /* capture reset + depth tables + persistent render into one graph */
   e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal);
   if (e) return fs_cuda_fail(ctx, e, "cudaStreamBeginCapture");
@@ -308,6 +322,17 @@ int fs_plan_run(fs_plan *p) {
   int e = cudaGraphLaunch(p->exec, ctx->stream);
   if (e) return fs_cuda_fail(ctx, e, "cudaGraphLaunch");
   ctx->launches += 2;
+  return FS_OK;
+}
+
+int fs_plan_kernel_ms(fs_plan *p, float *ms) {
+  if (!p || !ms) return FS_ERR_ARG;
+  fs_ctx *ctx = p->ctx;
+  if (!p->graph_ok) return fs_fail(ctx, FS_ERR_STATE, "plan has no graph");
+  cudaSetDevice(ctx->device);
+  int e = cudaEventSynchronize(p->ev_render[1]);
+  if (!e) e = cudaEventElapsedTime(ms, p->ev_render[0], p->ev_render[1]);
+  if (e) return fs_cuda_fail(ctx, e, "render kernel timing");
   return FS_OK;
 }
 

@@ -79,6 +79,7 @@ struct fs_plan {
   cudaGraph_t graph;
   cudaGraphExec_t exec;
   int32_t graph_ok;
+  cudaEvent_t ev_render[2]; /* recorded around the render kernel inside the graph */
 };
 
 int fs_fail(fs_ctx *ctx, int code, const char *fmt, ...);

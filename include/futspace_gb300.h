@@ -191,6 +191,10 @@ void fs_plan_free(fs_plan *plan);
 int fs_plan_set_cameras(fs_plan *plan, const fs_camera *cams, int32_t ncams);
 /* Enqueues one render of every view on the context stream. */
 int fs_plan_run(fs_plan *plan);
+/* Device time in ms of the persistent render kernel alone in the most recent
+ * fs_plan_run (events recorded inside the graph around that kernel); waits
+ * for that run to finish. */
+int fs_plan_kernel_ms(fs_plan *plan, float *ms);
 /* Renders with one plain launch pair per view instead (the comparison loop). */
 int fs_plan_run_per_view(fs_plan *plan);
 uint32_t *fs_plan_frame_dev(fs_plan *plan, int32_t view);
