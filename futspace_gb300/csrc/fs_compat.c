@@ -600,7 +600,7 @@ int futhark_entry_update_map(struct futhark_context *ctx, struct futhark_opaque_
   if (!ctx || !out0 || !in || !color_map || !height_map) return FS_ERR_ARG;
   const int64_t rows = height_map->shape[0], cols = height_map->shape[1];
   if (color_map->shape[0] != rows || color_map->shape[1] != cols || rows < 1 || cols < 1 ||
-      rows > 65536 || cols > 65536)
+      rows > 65536 || cols > 65536 || rows * cols > FS_MAX_TEXELS)
     return fs_fail(ctx->fs, FS_ERR_ARG, "update_map: colour %lldx%lld vs height %lldx%lld",
                    (long long)color_map->shape[0], (long long)color_map->shape[1],
                    (long long)rows, (long long)cols);

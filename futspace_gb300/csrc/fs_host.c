@@ -329,7 +329,7 @@ static int fs_map_build_pyramid(fs_ctx *ctx, fs_map *m) {
 
 static int fs_map_alloc(fs_ctx *ctx, fs_map **out, int64_t rows, int64_t cols) {
   if (!ctx || !out) return fs_fail(ctx, FS_ERR_ARG, "NULL argument");
-  if (rows <= 0 || cols <= 0 || rows > 65536 || cols > 65536)
+  if (rows <= 0 || cols <= 0 || rows > 65536 || cols > 65536 || rows * cols > FS_MAX_TEXELS)
     return fs_fail(ctx, FS_ERR_ARG, "map %lldx%lld out of range", (long long)rows,
                    (long long)cols);
   fs_map *m = (fs_map *)calloc(1, sizeof(fs_map));
@@ -409,7 +409,7 @@ int fs_map_wrap_device(fs_ctx *ctx, fs_map **out, const uint8_t *heights_dev,
                        const uint32_t *colors_dev, int64_t rows, int64_t cols) {
   if (!ctx || !out || !heights_dev || !colors_dev)
     return fs_fail(ctx, FS_ERR_ARG, "NULL argument");
-  if (rows <= 0 || cols <= 0 || rows > 65536 || cols > 65536)
+  if (rows <= 0 || cols <= 0 || rows > 65536 || cols > 65536 || rows * cols > FS_MAX_TEXELS)
     return fs_fail(ctx, FS_ERR_ARG, "map %lldx%lld out of range", (long long)rows,
                    (long long)cols);
   fs_map *m = (fs_map *)calloc(1, sizeof(fs_map));

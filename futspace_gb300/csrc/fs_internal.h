@@ -20,6 +20,8 @@ extern "C" {
 #define FS_MAX_ROWS 16383
 /* Largest depth-sample count per view (depth index packed in 20 bits). */
 #define FS_MAX_DEPTHS (1 << 20)
+/* Largest texel count of a map (the kernels index texels with 32-bit ints). */
+#define FS_MAX_TEXELS (1ll << 30)
 /* Maps bound to one launch. */
 #define FS_MAX_MAPS 4
 /* Levels of the height max pyramid (2^16 texels per side). */

@@ -80,7 +80,7 @@ __global__ void shadow_kernel(FsMapDev M, float s0, float s1, float s2, uint32_t
     if (lhs < -0.5f) count += 1;
   }
   const uint32_t black = 0xFF000000u; /* argb.black = from_rgba 0 0 0 1 */
-  const Channels ch{nullptr};
+  const DivChannels ch;
   out[(size_t)y * 1024 + x] = mix(ch, fm(step_size, (float)count), black, 1.0f,
                                   color_nearest(M, fx, fy));
 }

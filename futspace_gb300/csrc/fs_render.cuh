@@ -129,6 +129,11 @@ struct RenderShape {
  * mix(|row - y| / range, previous colour, |y - prev| / range, colour) with
  * range = max(1, prev - row); colour 0 becomes sky, with no gap fill.
  * Compiled for one lane per column and direct painting only. */
+template <bool B>
+struct BoolTag {
+  static constexpr bool value = B;
+};
+
 template <int TW, int LC, int U, int HF, int CF, int STG, int SM = 0>
 __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_blocks))
     render_kernel(const __grid_constant__ FsLaunch P) {
@@ -156,8 +161,8 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
   unsigned lanemask_lt;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lanemask_lt));
   for (int i = tid; i < 256; i += NT) lut[i] = __fdiv_rn((float)i, 255.0f);
-  const Channels chan{lut};
-  unsigned long long n_samples = 0, n_events = 0;
+  const LutChannels chan{lut};
+  uint32_t n_samples = 0, n_events = 0; /* work counters (ctx stats) */
 
   for (int iter = 0;; iter++) {
     int item;
@@ -179,10 +184,15 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
       tile = it & 4095;
     }
     const FsView *Vp = P.views ? P.views + vi : &P.view0;
+    /* the view's fields live in registers: the frame stores below may alias
+     * the view records as far as the compiler can tell */
     const float cam_h = Vp->cam_h, horizon = Vp->horizon;
     const int W = Vp->W, H = Vp->H, n = Vp->n;
     const uint32_t sky = Vp->sky, gap = Vp->gap;
+    const int vflags = Vp->flags;
     const FsMapDev &M = P.maps[Vp->map]; /* read in place: no local copy to index */
+    const HeightMap hmap{M.q, M.MW, M.MH};
+    const bool p2 = M.pow2 != 0;
     const float4 *zl = P.zline + Vp->zoff;
     const float *zi = P.zinvz + Vp->zoff;
     uint32_t *const out = Vp->out;
@@ -192,7 +202,9 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
     const bool valid = col < W;
     const float fcol = (float)col;
 
-    int m = H;          /* running minimum row of this column */
+    /* running minimum row of this column; 0 also marks a column past the
+     * frame's right edge, which never has an event */
+    int m = valid ? H : 0;
     int qh = 0, qt = 0; /* ring head / tail, warp-uniform */
     /* smoothing: the last event of this lane's column, queued once the sample
      * after it shows whether it held the minimum for a single sample */
@@ -202,16 +214,25 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
     auto sample_colour = [&](int k, int ecl) -> uint32_t {
       const float ec = (float)(c0 + ecl);
       const float4 L = __ldg(zl + k);
-      const float x = fa(L.x, fm(ec, L.z));
-      const float y = fa(L.y, fm(ec, L.w));
-      uint32_t colour = CF ? color_bilinear(M, chan, x, y) : color_nearest(M, x, y);
-      if (Vp->flags & (FSV_SHADE | FSV_FOG)) {
+      const float2 xy = axpy2(ec, make_float2(L.z, L.w), make_float2(L.x, L.y));
+      uint32_t colour = CF ? color_bilinear(M, chan, xy.x, xy.y) : color_nearest(M, xy.x, xy.y);
+      if (vflags & (FSV_SHADE | FSV_FOG)) {
         /* depth of sample k, as the depth table computes it */
         const float fi = (float)(k + 1);
         const float z = fm(fd(fi, 2.0f), fa(fm(2.0f, Vp->z0), fm(fs(fi, 1.0f), Vp->d)));
         colour = apply_effects(chan, *Vp, colour, z);
       }
       return colour;
+    };
+
+    /* screen row of depth sample k of this lane's column, clamped to [0, H] */
+    auto sample_row = [&](auto p2tag, int k) -> int {
+      constexpr bool P2 = decltype(p2tag)::value;
+      const float4 L = __ldg(zl + k);
+      const float2 xy = axpy2(fcol, make_float2(L.z, L.w), make_float2(L.x, L.y));
+      const float hh =
+          HF ? height_bilinear<P2>(hmap, xy.x, xy.y) : height_nearest<P2>(hmap, xy.x, xy.y);
+      return min(max(f2i(fa(fm(fs(cam_h, hh), __ldg(zi + k)), horizon)), 0), H);
     };
 
     /* colour the queued events [qh, qh+cnt) and paint their intervals */
@@ -253,28 +274,8 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
       __syncwarp();
     };
 
-    for (int k0 = 0; k0 < n; k0 += CH) {
-      if (__all_sync(FS_FULL_MASK, !valid || m == 0)) break;
-      if (M.pyr) {
-        /* Exact skip: rows are monotone in the height and in inv_z, so a row
-         * computed from an upper bound of every height in the chunk, at the
-         * chunk's nearest or farthest depth, bounds every sample's row from
-         * below. If that bound is not above the running minimum, no sample of
-         * the chunk can be an event for this column. */
-        const int ka = k0, kb = min(k0 + CH, n) - 1;
-        const float4 La = __ldg(zl + ka), Lb = __ldg(zl + kb);
-        const float iza = __ldg(zi + ka), izb = __ldg(zi + kb);
-        bool skip = !valid || m == 0;
-        if (!skip) {
-          const float xa = fa(La.x, fm(fcol, La.z)), ya = fa(La.y, fm(fcol, La.w));
-          const float xb = fa(Lb.x, fm(fcol, Lb.z)), yb = fa(Lb.y, fm(fcol, Lb.w));
-          const float dh = fs(cam_h, fa((float)segment_max_height(M, xa, ya, xb, yb), 1.0f));
-          const int ra = min(max(f2i(fa(fm(dh, iza), horizon)), 0), H);
-          const int rb = min(max(f2i(fa(fm(dh, izb), horizon)), 0), H);
-          skip = min(ra, rb) >= m;
-        }
-        if (__all_sync(FS_FULL_MASK, skip)) continue;
-      }
+    /* rows of one chunk of depth samples, then its events into the ring */
+    auto march_chunk = [&](auto p2tag, int k0) {
       int r[U];
       if constexpr (LC == 1) {
         /* one lane per column: every lane is at the same depth, so the depth
@@ -282,19 +283,8 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
 #pragma unroll
         for (int u = 0; u < U; u++) {
           const int k = k0 + u;
-          int rr = H;
-          if (k < n) {
-            const float4 L = __ldg(zl + k);
-            const float iz = __ldg(zi + k);
-            if (valid && m > 0) {
-              const float x = fa(L.x, fm(fcol, L.z));
-              const float y = fa(L.y, fm(fcol, L.w));
-              const float hh = HF ? height_bilinear(M, x, y) : height_nearest(M, x, y);
-              rr = min(max(f2i(fa(fm(fs(cam_h, hh), iz), horizon)), 0), H);
-              n_samples++;
-            }
-          }
-          r[u] = rr;
+          const int rr = sample_row(p2tag, min(k, n - 1));
+          r[u] = k < n ? rr : H;
         }
 #pragma unroll
         for (int u = 0; u < U; u++) {
@@ -329,17 +319,8 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
 #pragma unroll
         for (int u = 0; u < U; u++) {
           const int k = k0 + u * LC + dl;
-          int rr = H;
-          if (valid && m > 0 && k < n) {
-            const float4 L = __ldg(zl + k);
-            const float x = fa(L.x, fm(fcol, L.z));
-            const float y = fa(L.y, fm(fcol, L.w));
-            const float hh = HF ? height_bilinear(M, x, y) : height_nearest(M, x, y);
-            const float rel = fa(fm(fs(cam_h, hh), __ldg(zi + k)), horizon);
-            rr = min(max(f2i(rel), 0), H);
-            n_samples++;
-          }
-          r[u] = rr;
+          const int rr = sample_row(p2tag, min(k, n - 1));
+          r[u] = k < n ? rr : H;
         }
 #pragma unroll
         for (int u = 0; u < U; u++) {
@@ -362,33 +343,81 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
         }
       }
       __syncwarp();
-      while (qt - qh >= 32) {
-        drain(32);
-        qh += 32;
+    };
+
+    /* One loop, one drain site: march a chunk while fewer than 32 events wait,
+     * colour and paint 32 at a time, and flush the rest once the march ends. */
+    int k0 = 0;
+    bool marching = true;
+    for (;;) {
+      if (marching && qt - qh < 32) {
+        if (k0 >= n || __all_sync(FS_FULL_MASK, m == 0)) {
+          marching = false;
+          if constexpr (SM) {
+            /* the column's last event: no later sample is an event, so it held
+             * the minimum for a single sample only if it is the last sample */
+            const bool fin = pend_k >= 0;
+            const unsigned msk = __ballot_sync(FS_FULL_MASK, fin);
+            if (fin) {
+              const int pos = (qt + __popc(msk & lanemask_lt)) & (QCAP - 1);
+              const bool blend = (pend_k == n - 1) &&
+                                 (pend_kprev == pend_k - 1 || (pend_kprev < 0 && pend_k == 1));
+              q[pos * S::QW] = pack_event(pend_k, cl, pend_r, pend_p);
+              q[pos * S::QW + S::QW - 1] =
+                  (unsigned long long)(uint32_t)(pend_kprev + 1) | ((unsigned long long)blend << 32);
+            }
+            qt += __popc(msk);
+            __syncwarp();
+          }
+        } else {
+          const int kc = k0;
+          k0 += CH;
+          bool skip = false;
+          if (M.pyr) {
+            /* Exact skip: rows are monotone in the height and in inv_z, so a
+             * row computed from an upper bound of every height in the chunk,
+             * at the chunk's nearest or farthest depth, bounds every sample's
+             * row from below. If that bound is not above the running minimum,
+             * no sample of the chunk can be an event for this column. */
+            const int ka = kc, kb = min(kc + CH, n) - 1;
+            bool lskip = m == 0;
+            if (!lskip) {
+              const float4 La = __ldg(zl + ka), Lb = __ldg(zl + kb);
+              const float iza = __ldg(zi + ka), izb = __ldg(zi + kb);
+              const float2 xa = axpy2(fcol, make_float2(La.z, La.w), make_float2(La.x, La.y));
+              const float2 xb = axpy2(fcol, make_float2(Lb.z, Lb.w), make_float2(Lb.x, Lb.y));
+              const float dh =
+                  fs(cam_h, fa((float)segment_max_height(M, xa.x, xa.y, xb.x, xb.y), 1.0f));
+              const int ra = min(max(f2i(fa(fm(dh, iza), horizon)), 0), H);
+              const int rb = min(max(f2i(fa(fm(dh, izb), horizon)), 0), H);
+              lskip = min(ra, rb) >= m;
+            }
+            skip = __all_sync(FS_FULL_MASK, lskip);
+          }
+          if (!skip) {
+            if (P.stats && m > 0) {
+              int c = 0;
+#pragma unroll
+              for (int u = 0; u < U; u++) c += (kc + u * LC + dl < n) ? 1 : 0;
+              n_samples += (uint32_t)c;
+            }
+            if (p2)
+              march_chunk(BoolTag<true>{}, kc);
+            else
+              march_chunk(BoolTag<false>{}, kc);
+          }
+        }
+      }
+      const int avail = qt - qh;
+      if (avail >= 32 || (!marching && avail > 0)) {
+        const int cnt = min(avail, 32);
+        drain(cnt);
+        qh += cnt;
+      } else if (!marching) {
+        break;
       }
     }
-    if constexpr (SM) {
-      /* the column's last event: no later sample is an event, so it held the
-       * minimum for a single sample only if it is the last sample */
-      const bool fin = pend_k >= 0;
-      const unsigned msk = __ballot_sync(FS_FULL_MASK, fin);
-      if (fin) {
-        const int pos = (qt + __popc(msk & lanemask_lt)) & (QCAP - 1);
-        const bool blend = (pend_k == n - 1) &&
-                           (pend_kprev == pend_k - 1 || (pend_kprev < 0 && pend_k == 1));
-        q[pos * S::QW] = pack_event(pend_k, cl, pend_r, pend_p);
-        q[pos * S::QW + S::QW - 1] =
-            (unsigned long long)(uint32_t)(pend_kprev + 1) | ((unsigned long long)blend << 32);
-      }
-      qt += __popc(msk);
-      __syncwarp();
-      while (qt - qh >= 32) {
-        drain(32);
-        qh += 32;
-      }
-    }
-    if (qt > qh) drain(qt - qh);
-    n_events += (unsigned long long)qt;
+    n_events += (uint32_t)qt;
 
     if (STG) {
       /* gap fill + sky for this warp's columns, then the transposed store */
@@ -453,12 +482,12 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
   }
   if (STG && tid == 0) bulk_wait_all();
   if (P.stats) {
+    unsigned long long ns = n_samples;
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1)
-      n_samples += __shfl_down_sync(FS_FULL_MASK, n_samples, off);
+    for (int off = 16; off > 0; off >>= 1) ns += __shfl_down_sync(FS_FULL_MASK, ns, off);
     if (lane == 0) {
-      atomicAdd(reinterpret_cast<unsigned long long *>(P.stats), n_samples);
-      atomicAdd(reinterpret_cast<unsigned long long *>(P.stats) + 1, n_events);
+      atomicAdd(reinterpret_cast<unsigned long long *>(P.stats), ns);
+      atomicAdd(reinterpret_cast<unsigned long long *>(P.stats) + 1, (unsigned long long)n_events);
     }
   }
 }
