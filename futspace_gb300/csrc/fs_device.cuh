@@ -169,31 +169,45 @@ __device__ __forceinline__ int segment_max_height(const FsMapDev &M, float xa, f
 /* ---- matte 0.1.2 argb colour arithmetic (to_rgba / from_rgba / mix) ----------
  * A channel fetcher returns byte i of an ARGB word (0 blue, 1 green, 2 red,
  * 3 alpha) as the IEEE quotient byte / 255: from a 256-entry table of those
- * quotients in shared memory, or from the division itself. */
+ * quotients in shared memory, or from the division itself. `bits(v)` takes
+ * the byte from a channel held as the bit pattern of the float 2^23 + byte. */
 struct LutChannels {
   const float *lut;
   __device__ __forceinline__ float operator()(uint32_t c, int i) const {
     return lut[__byte_perm(c, 0u, 0x4440u + (uint32_t)i)];
   }
+  __device__ __forceinline__ float bits(uint32_t v) const { return lut[v - 0x4B000000u]; }
 };
 struct DivChannels {
   __device__ __forceinline__ float operator()(uint32_t c, int i) const {
     return fd((float)__byte_perm(c, 0u, 0x4440u + (uint32_t)i), 255.0f);
   }
+  __device__ __forceinline__ float bits(uint32_t v) const {
+    return fd(fs(__uint_as_float(v), 8388608.0f), 255.0f);
+  }
+};
+
+/* A colour between two mixes: each channel byte as the bit pattern of the float
+ * 2^23 + byte. */
+struct Argb {
+  uint32_t r, g, b, a;
 };
 
 /* from_rgba of channel pairs (r, g) and (b, a), each already clamped to
  * [0, 1]: byte = trunc(v * 255). v * 255 lies in [0, 255], so adding 2^23 with
  * round-toward-zero leaves trunc(v * 255) in the low mantissa bits. */
-__device__ __forceinline__ uint32_t pack_argb(float2 rg, float2 ba) {
+__device__ __forceinline__ Argb to_bytes(float2 rg, float2 ba) {
   const float2 k255 = make_float2(255.0f, 255.0f);
   const float2 srg = mul2(rg, k255), sba = mul2(ba, k255);
-  const uint32_t r = __float_as_uint(__fadd_rz(srg.x, 8388608.0f));
-  const uint32_t g = __float_as_uint(__fadd_rz(srg.y, 8388608.0f));
-  const uint32_t b = __float_as_uint(__fadd_rz(sba.x, 8388608.0f));
-  const uint32_t a = __float_as_uint(__fadd_rz(sba.y, 8388608.0f));
-  return __byte_perm(__byte_perm(b, g, 0x0040u), __byte_perm(r, a, 0x0040u), 0x5410u);
+  return Argb{__float_as_uint(__fadd_rz(srg.x, 8388608.0f)),
+              __float_as_uint(__fadd_rz(srg.y, 8388608.0f)),
+              __float_as_uint(__fadd_rz(sba.x, 8388608.0f)),
+              __float_as_uint(__fadd_rz(sba.y, 8388608.0f))};
 }
+__device__ __forceinline__ uint32_t pack(const Argb &c) {
+  return __byte_perm(__byte_perm(c.b, c.g, 0x0040u), __byte_perm(c.r, c.a, 0x0040u), 0x5410u);
+}
+__device__ __forceinline__ uint32_t pack_argb(float2 rg, float2 ba) { return pack(to_bytes(rg, ba)); }
 
 /* mix's weight normalisation w1 / (w1 + w2), w2 / (w1 + w2): when the sum is
  * exactly 1 the quotients are the weights themselves. */
@@ -207,18 +221,23 @@ __device__ __forceinline__ void mix_weights(float w1, float w2, float &w1n, floa
   }
 }
 
-/* argb.mix with normalised weights: per channel c1*w1n + c2*w2n, clamped to
- * [0, 1] (a NaN channel gives byte 0), times 255, truncated. */
-template <class Ch>
-__device__ __forceinline__ uint32_t mix_n(const Ch &ch, float w1n, uint32_t c1, float w2n,
-                                          uint32_t c2) {
+/* argb.mix with normalised weights on channel values: per channel
+ * c1*w1n + c2*w2n, clamped to [0, 1] (a NaN channel gives byte 0), times 255,
+ * truncated. */
+__device__ __forceinline__ Argb mix_ch(float w1n, float2 rg1, float2 ba1, float w2n, float2 rg2,
+                                       float2 ba2) {
   const float2 W1 = make_float2(w1n, w1n), W2 = make_float2(w2n, w2n);
-  const float2 p_rg = mul2(make_float2(ch(c1, 2), ch(c1, 1)), W1);
-  const float2 q_rg = mul2(make_float2(ch(c2, 2), ch(c2, 1)), W2);
-  const float2 p_ba = mul2(make_float2(ch(c1, 0), ch(c1, 3)), W1);
-  const float2 q_ba = mul2(make_float2(ch(c2, 0), ch(c2, 3)), W2);
-  return pack_argb(make_float2(sat_add(p_rg.x, q_rg.x), sat_add(p_rg.y, q_rg.y)),
-                   make_float2(sat_add(p_ba.x, q_ba.x), sat_add(p_ba.y, q_ba.y)));
+  const float2 p_rg = mul2(rg1, W1), q_rg = mul2(rg2, W2);
+  const float2 p_ba = mul2(ba1, W1), q_ba = mul2(ba2, W2);
+  return to_bytes(make_float2(sat_add(p_rg.x, q_rg.x), sat_add(p_rg.y, q_rg.y)),
+                  make_float2(sat_add(p_ba.x, q_ba.x), sat_add(p_ba.y, q_ba.y)));
+}
+
+template <class Ch>
+__device__ __forceinline__ Argb mix_n(const Ch &ch, float w1n, uint32_t c1, float w2n,
+                                      uint32_t c2) {
+  return mix_ch(w1n, make_float2(ch(c1, 2), ch(c1, 1)), make_float2(ch(c1, 0), ch(c1, 3)), w2n,
+                make_float2(ch(c2, 2), ch(c2, 1)), make_float2(ch(c2, 0), ch(c2, 3)));
 }
 
 template <class Ch>
@@ -226,7 +245,7 @@ __device__ __forceinline__ uint32_t mix(const Ch &ch, float w1, uint32_t c1, flo
                                         uint32_t c2) {
   float w1n, w2n;
   mix_weights(w1, w2, w1n, w2n);
-  return mix_n(ch, w1n, c1, w2n, c2);
+  return pack(mix_n(ch, w1n, c1, w2n, c2));
 }
 
 /* matte colourspace.scale: RGB times s, alpha kept, then from_rgba. */
@@ -266,9 +285,15 @@ __device__ __forceinline__ uint32_t color_bilinear(const FsMapDev &M, const Ch &
   const uint32_t c10 = __ldg(r1 + ix0), c11 = __ldg(r1 + ix1);
   float w0, w1;
   mix_weights(fs(cx, x), fs(x, fx), w0, w1);
-  const uint32_t x1 = mix_n(ch, w0, c00, w1, c01);
-  const uint32_t x2 = mix_n(ch, w0, c10, w1, c11);
-  return mix(ch, fs(cy, y), x1, fs(y, fy), x2);
+  const Argb x1 = mix_n(ch, w0, c00, w1, c01);
+  const Argb x2 = mix_n(ch, w0, c10, w1, c11);
+  /* the y mix reads the channels of x1 and x2 straight from their bytes */
+  float v0, v1;
+  mix_weights(fs(cy, y), fs(y, fy), v0, v1);
+  return pack(mix_ch(v0, make_float2(ch.bits(x1.r), ch.bits(x1.g)),
+                     make_float2(ch.bits(x1.b), ch.bits(x1.a)), v1,
+                     make_float2(ch.bits(x2.r), ch.bits(x2.g)),
+                     make_float2(ch.bits(x2.b), ch.bits(x2.a))));
 }
 
 /* png_color, fut/render_functions.fut:91-92 */

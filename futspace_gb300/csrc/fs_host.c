@@ -553,7 +553,7 @@ int fs_render_device(fs_ctx *ctx, const fs_map *map, const fs_camera *cam,
   int rc = fs_make_view(ctx, cam, params ? params : &dp, width, height, 0, &v);
   if (rc) return rc;
   cudaSetDevice(ctx->device);
-  rc = fs_ensure_ztable(ctx, v.n);
+  rc = fs_ensure_ztable(ctx, (int64_t)v.n + FS_ZPAD);
   if (rc) return rc;
   v.out = out_dev;
   return fs_render_view(ctx, &map->dev, &v, NULL, ctx->zline, ctx->zinvz, NULL);

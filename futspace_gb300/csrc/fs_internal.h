@@ -22,6 +22,10 @@ extern "C" {
 #define FS_MAX_DEPTHS (1 << 20)
 /* Largest texel count of a map (the kernels index texels with 32-bit ints). */
 #define FS_MAX_TEXELS (1ll << 30)
+/* Readable depth-table entries past the n samples of every view's slice: the
+ * render kernel loads whole chunks of depths (at most FS_ZPAD) without a bound
+ * check and discards the rows of depths past n. The entries are zeros. */
+#define FS_ZPAD 64
 /* Maps bound to one launch. */
 #define FS_MAX_MAPS 4
 /* Levels of the height max pyramid (2^16 texels per side). */

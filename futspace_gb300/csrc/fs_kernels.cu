@@ -38,7 +38,13 @@ __device__ __forceinline__ void ztable_fill(const FsView *Vp, float4 *zline, flo
   const float a4 = fs(-s, fm(c, v)); /* right_y / z */
   float4 *zl = zline + Vp->zoff;
   float *zi = zinvz + Vp->zoff;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n + FS_ZPAD;
+       k += gridDim.x * blockDim.x) {
+    if (k >= n) {
+      zl[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      zi[k] = 0.0f;
+      continue;
+    }
     const float fi = (float)(k + 1);
     const float z = fm(fd(fi, 2.0f), fa(fm(2.0f, z0), fm(fs(fi, 1.0f), d)));
     const float lx = fm(a1, z), ly = fm(a2, z), rx = fm(a3, z), ry = fm(a4, z);

@@ -16,7 +16,7 @@
  *  - at most FS_NOALLOC_MAX_DEPTHS depth samples per frame (65536: draw
  *    distances up to about 2.1 million map units with the default depth step);
  *    longer schedules are rejected with FS_ERR_ARG;
- *  - the array (1.25 MiB) stays allocated on every GPU that loads the library
+ *  - the array (about 1.25 MiB) stays allocated on every GPU that loads the library
  *    until the process exits;
  *  - all calls share it: each call rewrites the entries it reads before reading
  *    them (nothing needs to start at zero), so calls that overlap on the GPU --
@@ -34,8 +34,9 @@
 
 #define FS_NOALLOC_MAX_DEPTHS 65536
 
-/* [FS_NOALLOC_MAX_DEPTHS] float4 {x0, y0, dx, dy}, then [FS_NOALLOC_MAX_DEPTHS] float inv_z */
-static __device__ __align__(256) unsigned char fs_noalloc_scratch[FS_NOALLOC_MAX_DEPTHS * 20];
+/* [FS_NOALLOC_MAX_DEPTHS + FS_ZPAD] float4 {x0, y0, dx, dy}, then as many float inv_z */
+#define FS_NOALLOC_ENTRIES (FS_NOALLOC_MAX_DEPTHS + FS_ZPAD)
+static __device__ __align__(256) unsigned char fs_noalloc_scratch[FS_NOALLOC_ENTRIES * 20];
 
 /* Device address of fs_noalloc_scratch per device ordinal. In host code the
  * array's name only stands in for it; the kernels must be given this address. */
@@ -76,7 +77,7 @@ extern "C" int fs_render_device_noalloc(fs_ctx *ctx, const fs_map *map, const fs
   if (rc) return rc;
   float4 *zline = reinterpret_cast<float4 *>(scratch);
   float *zinvz = reinterpret_cast<float *>(static_cast<unsigned char *>(scratch) +
-                                           sizeof(float4) * FS_NOALLOC_MAX_DEPTHS);
+                                           sizeof(float4) * FS_NOALLOC_ENTRIES);
   v.out = out_dev;
   return fs_render_view(ctx, &map->dev, &v, nullptr, zline, zinvz, nullptr);
 }

@@ -246,7 +246,7 @@ int fs_plan_new(fs_ctx *ctx, fs_plan **out, const fs_map *const *maps, int32_t n
     }
     p->fv_h[v].zoff = zoff;
     p->ncap[v] = p->fv_h[v].n;
-    zoff += p->fv_h[v].n;
+    zoff += p->fv_h[v].n + FS_ZPAD;
     p->offsets[v] = px;
     px += ((int64_t)vw->width * vw->height + 63) & ~(int64_t)63; /* 256-byte aligned frames */
     if (vw->height > hmax) hmax = vw->height;

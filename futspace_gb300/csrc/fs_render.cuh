@@ -144,6 +144,7 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
   constexpr int QCAP = S::QCAP;
   static_assert(NT % 32 == 0 && 32 % LC == 0 && TW % 4 == 0 && TW <= 128, "shape");
   static_assert(!SM || (LC == 1 && STG == 0), "smoothing: one lane per column, direct paint");
+  static_assert(CH <= FS_ZPAD, "a chunk reads at most FS_ZPAD depth-table entries past n");
 
   extern __shared__ __align__(1024) unsigned char smem[];
   uint32_t *box = reinterpret_cast<uint32_t *>(smem);
@@ -283,7 +284,7 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
 #pragma unroll
         for (int u = 0; u < U; u++) {
           const int k = k0 + u;
-          const int rr = sample_row(p2tag, min(k, n - 1));
+          const int rr = sample_row(p2tag, k);
           r[u] = k < n ? rr : H;
         }
 #pragma unroll
@@ -319,7 +320,7 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
 #pragma unroll
         for (int u = 0; u < U; u++) {
           const int k = k0 + u * LC + dl;
-          const int rr = sample_row(p2tag, min(k, n - 1));
+          const int rr = sample_row(p2tag, k);
           r[u] = k < n ? rr : H;
         }
 #pragma unroll

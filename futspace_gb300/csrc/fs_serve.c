@@ -222,7 +222,7 @@ int fs_server_new(fs_ctx *ctx, fs_server **out, const fs_map *const *maps, int32
   }
   s->grid = occ * ctx->sm_count;
   if (t.ctas > 0 && t.ctas < s->grid) s->grid = t.ctas;
-  const size_t zcnt = (size_t)cfg->nsessions * (size_t)cfg->max_depths;
+  const size_t zcnt = (size_t)cfg->nsessions * ((size_t)cfg->max_depths + FS_ZPAD);
   s->sess_busy = (int8_t *)calloc((size_t)cfg->nsessions, 1);
   s->slots = (fs_slot *)calloc((size_t)cfg->slots, sizeof(fs_slot));
   if (!s->sess_busy || !s->slots || !arena_init(&s->arena, cfg->budget_bytes) ||
@@ -306,7 +306,7 @@ static int launch_batch(fs_server *s, fs_slot *sl, fs_request *reqs, fs_fifo *re
       st->errors++;
       continue;
     }
-    v.zoff = (int64_t)r->session * s->cfg.max_depths;
+    v.zoff = (int64_t)r->session * ((int64_t)s->cfg.max_depths + FS_ZPAD);
     v.out = (uint32_t *)(s->arena_base + frame_off[ri]);
     v.tmap = -1;
     packed[nb] = v;
