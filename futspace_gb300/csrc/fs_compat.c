@@ -540,7 +540,7 @@ int futhark_entry_render(struct futhark_context *ctx, struct futhark_u32_2d **ou
   FsView v;
   int rc = fs_make_view(ctx->fs, &in->cam, &p, W, H, 0, &v);
   if (rc) return rc;
-  rc = fs_ensure_ztable(ctx->fs, (int64_t)v.n + FS_ZPAD);
+  rc = fs_ensure_ztable(ctx->fs, v.n);
   if (rc) return rc;
   struct futhark_u32_2d *a = (struct futhark_u32_2d *)calloc(1, sizeof(*a));
   if (!a) return fs_fail(ctx->fs, FS_ERR_NOMEM, "render: out of memory");

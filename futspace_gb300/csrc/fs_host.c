@@ -267,7 +267,9 @@ int fs_ctx_stats(fs_ctx *ctx, int32_t enable, uint64_t out2[2]) {
   return FS_OK;
 }
 
+/* Depth table for one view of n samples, plus the FS_ZPAD entries past them. */
 int fs_ensure_ztable(fs_ctx *ctx, int64_t n) {
+  n += FS_ZPAD;
   if (n <= ctx->zcap) return FS_OK;
   int64_t cap = n < 4096 ? 4096 : n;
   cudaStreamSynchronize(ctx->stream);
@@ -489,6 +491,19 @@ int fs_tune_fits(fs_ctx *ctx, const FsTune *t, int32_t stride_max) {
   return fsk_render_smem(t, stride_max) <= ctx->smem_optin;
 }
 
+/* The kernel mode a view needs (smoothing, shading/fog epilogue) applied to a
+ * tuning; a tuning with no kernel compiled for that mode becomes the mode's
+ * default configuration. */
+FsTune fs_tune_for_mode(FsTune t, int32_t view_flags) {
+  t.smooth = (view_flags & FSV_SMOOTH) ? 1 : 0;
+  t.fx = (view_flags & (FSV_SHADE | FSV_FOG)) ? 1 : 0;
+  if ((t.smooth || t.fx) && !fsk_tune_supported(&t)) {
+    const FsTune d = {128, 1, t.smooth ? 4 : 8, 0, t.ctas, t.smooth, t.fx};
+    t = d;
+  }
+  return t;
+}
+
 /* Default choice when the tuning cache has no entry: the first table entry
  * whose shared-memory stage fits. */
 FsTune fs_default_tune(fs_ctx *ctx, int32_t stride_max) {
@@ -508,11 +523,7 @@ int fs_render_view(fs_ctx *ctx, const FsMapDev *map, FsView *v, const FsTune *tu
   else if (ctx->forced.tw) t = ctx->forced;
   else if (!fs_tune_lookup(ctx, v->W, v->H, map->MH, map->MW, v->flags, &t))
     t = fs_default_tune(ctx, stride);
-  t.smooth = (v->flags & FSV_SMOOTH) ? 1 : 0;
-  if (t.smooth && !fsk_tune_supported(&t)) {
-    const FsTune sm = {64, 1, 4, 0, 0, 1}; /* smoothing kernels: one lane per column */
-    t = sm;
-  }
+  t = fs_tune_for_mode(t, v->flags);
   if (!t.tw || !fs_tune_fits(ctx, &t, stride))
     return fs_fail(ctx, FS_ERR_ARG, "no kernel configuration fits screen height %d", v->H);
   FsLaunch launch;
@@ -553,7 +564,7 @@ int fs_render_device(fs_ctx *ctx, const fs_map *map, const fs_camera *cam,
   int rc = fs_make_view(ctx, cam, params ? params : &dp, width, height, 0, &v);
   if (rc) return rc;
   cudaSetDevice(ctx->device);
-  rc = fs_ensure_ztable(ctx, (int64_t)v.n + FS_ZPAD);
+  rc = fs_ensure_ztable(ctx, v.n);
   if (rc) return rc;
   v.out = out_dev;
   return fs_render_view(ctx, &map->dev, &v, NULL, ctx->zline, ctx->zinvz, NULL);

@@ -102,6 +102,7 @@ typedef struct {
   int32_t stage; /* 1: shared-memory column stage + TMA store; 0: direct painting */
   int32_t ctas;  /* persistent CTAs (0: as many as fit) */
   int32_t smooth; /* 1: the `#on` smoothing kernels (FS_TUNE_LIST_SM) */
+  int32_t fx;     /* 1: kernels with the shading / fog epilogue compiled in */
 } FsTune;
 
 /* Kernel-side entry points (fs_kernels.cu). Each returns a cudaError_t. */

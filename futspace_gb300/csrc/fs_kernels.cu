@@ -152,13 +152,15 @@ extern "C" int fsk_serve_prepare(const FsView *packed_dev, const int32_t *ids_de
 
 extern "C" int fsk_tune_supported(const FsTune *t) {
 #define FS_CASE(TW_, LC_, U_, STG_) \
-  if (t->tw == TW_ && t->lc == LC_ && t->u == U_ && t->stage == STG_ && !t->smooth) return 1;
-#define FS_CASE_SMOOTH(TW_, LC_, U_, STG_) \
-  if (t->tw == TW_ && t->lc == LC_ && t->u == U_ && t->stage == STG_ && t->smooth) return 1;
+  if (t->tw == TW_ && t->lc == LC_ && t->u == U_ && t->stage == STG_ && !t->smooth && !t->fx) return 1;
+#define FS_CASE_M(TW_, LC_, U_, STG_, SM_, FX_)                                                \
+  if (t->tw == TW_ && t->lc == LC_ && t->u == U_ && t->stage == STG_ && t->smooth == SM_ && \
+      t->fx == FX_)                                                                         \
+    return 1;
   FS_TUNE_LIST(FS_CASE)
-  FS_TUNE_LIST_SM(FS_CASE_SMOOTH)
+  FS_TUNE_LIST_MODES(FS_CASE_M)
 #undef FS_CASE
-#undef FS_CASE_SMOOTH
+#undef FS_CASE_M
   return 0;
 }
 

@@ -275,11 +275,7 @@ int fs_plan_new(fs_ctx *ctx, fs_plan **out, const fs_map *const *maps, int32_t n
     fs_plan_free(p);
     return fs_fail(ctx, FS_ERR_ARG, "no kernel configuration fits screen height %d", hmax);
   }
-  if (params->smoothing) {
-    const FsTune sm = {128, 1, 4, 0, 0, 1}; /* smoothing kernels: one lane per column */
-    t = sm;
-  }
-  p->tune = t;
+  p->tune = fs_tune_for_mode(t, p->fv_h[0].flags);
   rc = plan_build(p);
   if (rc) {
     fs_plan_free(p);
@@ -390,7 +386,9 @@ int fs_plan_get_tune(const fs_plan *p, int32_t out5[5]) {
 
 int fs_plan_set_tune(fs_plan *p, const int32_t tune5[5]) {
   if (!p || !tune5) return FS_ERR_ARG;
-  FsTune t = {tune5[0], tune5[1], tune5[2], tune5[3], tune5[4], p->params.smoothing ? 1 : 0};
+  FsTune t = {tune5[0], tune5[1], tune5[2], tune5[3], tune5[4], 0, 0};
+  t.smooth = (p->fv_h[0].flags & FSV_SMOOTH) ? 1 : 0;
+  t.fx = (p->fv_h[0].flags & (FSV_SHADE | FSV_FOG)) ? 1 : 0;
   if (!fs_tune_fits(p->ctx, &t, p->stride_max))
     return fs_fail(p->ctx, FS_ERR_ARG, "tuning (%d,%d,%d,%d) unsupported or too large", t.tw,
                    t.lc, t.u, t.stage);

@@ -94,6 +94,7 @@ int fs_encode_frame_map(fs_ctx *ctx, uint32_t *frame, int32_t W, int32_t H, int3
 int fs_render_view(fs_ctx *ctx, const FsMapDev *map, FsView *v, const FsTune *tune,
                    float4 *zline, float *zinvz, const CUtensorMap *tmap_pre);
 int fs_tune_fits(fs_ctx *ctx, const FsTune *t, int32_t stride_max);
+FsTune fs_tune_for_mode(FsTune t, int32_t view_flags);
 FsTune fs_default_tune(fs_ctx *ctx, int32_t stride_max);
 int fs_tune_count(void);
 int fs_tune_get(int i, int32_t out5[5]);

@@ -128,13 +128,14 @@ struct RenderShape {
  * is none and the event is sample 1). The blend of row y in [row, prev) is
  * mix(|row - y| / range, previous colour, |y - prev| / range, colour) with
  * range = max(1, prev - row); colour 0 becomes sky, with no gap fill.
- * Compiled for one lane per column and direct painting only. */
+ * Compiled for one lane per column and direct painting only.
+ * FX = 1: the optional shading / fog epilogue (views with FSV_SHADE/FSV_FOG). */
 template <bool B>
 struct BoolTag {
   static constexpr bool value = B;
 };
 
-template <int TW, int LC, int U, int HF, int CF, int STG, int SM = 0>
+template <int TW, int LC, int U, int HF, int CF, int STG, int SM, int FX>
 __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_blocks))
     render_kernel(const __grid_constant__ FsLaunch P) {
   using S = RenderShape<TW, LC, U, STG, SM>;
@@ -217,11 +218,13 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
       const float4 L = __ldg(zl + k);
       const float2 xy = axpy2(ec, make_float2(L.z, L.w), make_float2(L.x, L.y));
       uint32_t colour = CF ? color_bilinear(M, chan, xy.x, xy.y) : color_nearest(M, xy.x, xy.y);
-      if (vflags & (FSV_SHADE | FSV_FOG)) {
-        /* depth of sample k, as the depth table computes it */
-        const float fi = (float)(k + 1);
-        const float z = fm(fd(fi, 2.0f), fa(fm(2.0f, Vp->z0), fm(fs(fi, 1.0f), Vp->d)));
-        colour = apply_effects(chan, *Vp, colour, z);
+      if constexpr (FX) {
+        if (vflags & (FSV_SHADE | FSV_FOG)) {
+          /* depth of sample k, as the depth table computes it */
+          const float fi = (float)(k + 1);
+          const float z = fm(fd(fi, 2.0f), fa(fm(2.0f, Vp->z0), fm(fs(fi, 1.0f), Vp->d)));
+          colour = apply_effects(chan, *Vp, colour, z);
+        }
       }
       return colour;
     };
@@ -495,11 +498,18 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
 
 }  // namespace fsd
 
-/* Configurations compiled with the `#on` smoothing branch (one lane per column,
- * direct painting), for every filter pair. */
-#define FS_TUNE_LIST_SM(X) \
-  X(64, 1, 4, 0)           \
-  X(128, 1, 4, 0)
+/* Kernel modes beyond the plain render, each compiled for a few configurations
+ * and every filter pair: (TW, LC, U, STG, smoothing, epilogue). The epilogue
+ * is its own instantiation because its code, present but unused, makes the
+ * plain kernel measurably slower. */
+#define FS_TUNE_LIST_MODES(X) \
+  X(64, 1, 4, 0, 0, 1)        \
+  X(128, 1, 4, 0, 0, 1)       \
+  X(128, 1, 8, 0, 0, 1)       \
+  X(64, 1, 4, 0, 1, 0)        \
+  X(128, 1, 4, 0, 1, 0)       \
+  X(64, 1, 4, 0, 1, 1)        \
+  X(128, 1, 4, 0, 1, 1)
 
 /* The tuning table: (TW, LC, U, STG) compiled for every filter pair. */
 #define FS_TUNE_LIST(X) \

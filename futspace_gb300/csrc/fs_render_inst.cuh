@@ -1,6 +1,6 @@
 /*
  * Instantiates the render kernel for one (height filter, colour filter) pair
- * and every tuning triple of FS_TUNE_LIST. Included by fs_render_h?c?.cu with
+ * and every configuration of FS_TUNE_LIST and FS_TUNE_LIST_MODES. Included by fs_render_h?c?.cu with
  * FS_HF, FS_CF and FS_RENDER_ENTRY defined, so the four pairs compile as
  * separate translation units in parallel.
  *
@@ -14,12 +14,12 @@ extern "C" int FS_RENDER_ENTRY(int op, const FsLaunch *L, const FsTune *t, int g
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return (int)e;
   if (dev < 0 || dev >= 64) return (int)cudaErrorInvalidDevice;
-#define FS_CASE(TW_, LC_, U_, STG_) FS_CASE_SM(TW_, LC_, U_, STG_, 0)
-#define FS_CASE_SMOOTH(TW_, LC_, U_, STG_) FS_CASE_SM(TW_, LC_, U_, STG_, 1)
-#define FS_CASE_SM(TW_, LC_, U_, STG_, SM_)                                                 \
-  if (t->tw == TW_ && t->lc == LC_ && t->u == U_ && t->stage == STG_ && t->smooth == SM_) { \
+#define FS_CASE(TW_, LC_, U_, STG_) FS_CASE_M(TW_, LC_, U_, STG_, 0, 0)
+#define FS_CASE_M(TW_, LC_, U_, STG_, SM_, FX_)                                              \
+  if (t->tw == TW_ && t->lc == LC_ && t->u == U_ && t->stage == STG_ && t->smooth == SM_ &&  \
+      t->fx == FX_) {                                                                       \
     static int smem_set[64];                                                               \
-    auto kern = fsd::render_kernel<TW_, LC_, U_, FS_HF, FS_CF, STG_, SM_>;                 \
+    auto kern = fsd::render_kernel<TW_, LC_, U_, FS_HF, FS_CF, STG_, SM_, FX_>;             \
     if (smem_set[dev] < (int)smem) {                                                       \
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
       if (e != cudaSuccess) return (int)e;                                                 \
@@ -31,9 +31,8 @@ extern "C" int FS_RENDER_ENTRY(int op, const FsLaunch *L, const FsTune *t, int g
     return (int)cudaGetLastError();                                                        \
   }
   FS_TUNE_LIST(FS_CASE)
-  FS_TUNE_LIST_SM(FS_CASE_SMOOTH)
+  FS_TUNE_LIST_MODES(FS_CASE_M)
 #undef FS_CASE
-#undef FS_CASE_SMOOTH
-#undef FS_CASE_SM
+#undef FS_CASE_M
   return (int)cudaErrorInvalidValue;
 }

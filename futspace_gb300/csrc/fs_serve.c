@@ -203,10 +203,18 @@ int fs_server_new(fs_ctx *ctx, fs_server **out, const fs_map *const *maps, int32
     FsTune def = {128, 1, 4, 0, 0};
     t = def;
   }
-  if (params->smoothing) {
-    const FsTune sm = {128, 1, 4, 0, 0, 1};
-    if (!cfg->tune[0]) t = sm;
-    t.smooth = 1;
+  {
+    /* the mode (smoothing, epilogue) follows the parameters; an explicit
+     * tuning must have a kernel compiled for it */
+    const int32_t flags = (params->smoothing ? FSV_SMOOTH : 0) |
+                          ((params->effects & FS_FX_SHADE) ? FSV_SHADE : 0) |
+                          ((params->effects & FS_FX_FOG) ? FSV_FOG : 0);
+    if (cfg->tune[0]) {
+      t.smooth = (flags & FSV_SMOOTH) ? 1 : 0;
+      t.fx = (flags & (FSV_SHADE | FSV_FOG)) ? 1 : 0;
+    } else {
+      t = fs_tune_for_mode(t, flags);
+    }
   }
   if (t.stage != 0 || !fsk_tune_supported(&t)) {
     fs_server_free(s);

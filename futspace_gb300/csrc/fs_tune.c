@@ -151,7 +151,8 @@ int fs_autotune_frame(fs_ctx *ctx, const fs_map *map, const fs_camera *cam,
   for (int i = 0; i < fs_tune_count(); i++) {
     int32_t t5[5];
     fs_tune_get(i, t5);
-    FsTune t = {t5[0], t5[1], t5[2], t5[3], 0, (j.view.flags & FSV_SMOOTH) ? 1 : 0};
+    FsTune t = {t5[0], t5[1], t5[2], t5[3], 0, (j.view.flags & FSV_SMOOTH) ? 1 : 0,
+                (j.view.flags & (FSV_SHADE | FSV_FOG)) ? 1 : 0};
     if (!fs_tune_fits(ctx, &t, height | 1)) continue;
     j.tune = t;
     float ms = 0.0f;
@@ -192,7 +193,8 @@ int fs_plan_autotune(fs_plan *p, int32_t reps, int32_t out5[5], float *best_ms) 
   for (int i = 0; i < fs_tune_count(); i++) {
     int32_t t5[5];
     fs_tune_get(i, t5);
-    FsTune t = {t5[0], t5[1], t5[2], t5[3], 0, p->params.smoothing ? 1 : 0};
+    FsTune t = {t5[0], t5[1], t5[2], t5[3], 0, (p->fv_h[0].flags & FSV_SMOOTH) ? 1 : 0,
+                (p->fv_h[0].flags & (FSV_SHADE | FSV_FOG)) ? 1 : 0};
     if (!fs_tune_fits(ctx, &t, p->stride_max)) continue;
     rc = fs_plan_set_tune(p, t5);
     if (rc) break;
