@@ -542,12 +542,14 @@ int fs_render_view(fs_ctx *ctx, const FsMapDev *map, FsView *v, const FsTune *tu
   L->zline = zline;
   L->zinvz = zinvz;
   L->stats = ctx->stats_dev;
-  L->nitems = (v->W + t.tw - 1) / t.tw;
+  L->nitems = (v->W + fsk_item_width(&t) - 1) / fsk_item_width(&t);
   L->stride_max = stride;
+  const int32_t per_cta = fsk_items_per_cta(&t);
   int e = fsk_ztable(NULL, &L->view0, 1, v->n, zline, zinvz, ctx->stream);
   if (e) return fs_cuda_fail(ctx, e, "z-table kernel launch");
   e = fsk_render(L, &t, (v->flags & FSV_HEIGHT_BILINEAR) != 0,
-                 (v->flags & FSV_COLOR_BILINEAR) != 0, L->nitems, ctx->stream);
+                 (v->flags & FSV_COLOR_BILINEAR) != 0, (L->nitems + per_cta - 1) / per_cta,
+                 ctx->stream);
   if (e) return fs_cuda_fail(ctx, e, "render kernel launch");
   ctx->launches += 2;
   return FS_OK;

@@ -116,6 +116,11 @@ size_t fsk_render_smem(const FsTune *t, int32_t stride_max);
 int fsk_render_max_ctas_per_sm(const FsTune *t, int32_t hf, int32_t cf, int32_t stride_max,
                                int32_t *out);
 int fsk_tune_supported(const FsTune *t);
+int32_t fsk_item_width(const FsTune *t);
+int32_t fsk_items_per_cta(const FsTune *t);
+/* Work items pack (view or session << 16) | column tile or strip. */
+#define FS_ITEM_VIEWS 32768
+#define FS_ITEM_TILES 65536
 int fsk_shadowmap(const FsMapDev *map, const float sun[3], uint32_t *out, cudaStream_t st);
 int fsk_mask_heights(const int32_t *in, uint8_t *out, int64_t count, cudaStream_t st);
 int fsk_build_quads(const uint8_t *h, uint32_t *q, int32_t MH, int32_t MW, cudaStream_t st);

@@ -169,8 +169,16 @@ extern "C" size_t fsk_render_smem(const FsTune *t, int32_t stride_max) {
   const size_t nw = (size_t)t->tw * t->lc / 32;
   const size_t box = t->stage ? 2ull * kBoxRows * t->tw * 4 : 0;
   const size_t stage = t->stage ? (size_t)t->tw * stride_max * 4 : 0;
-  return box + nw * queue_cap(t->u) * 8 * (t->smooth ? 2 : 1) + 256 * 4 + (size_t)t->tw * 8 +
-         stage;
+  return box + nw * queue_cap(t->u) * 8 * (t->smooth ? 2 : 1) + 256 * 4 + stage;
+}
+
+/* Screen columns per work item: a CTA tile with the shared-memory stage, a
+ * warp strip with direct painting. */
+extern "C" int32_t fsk_item_width(const FsTune *t) { return t->stage ? t->tw : 32 / t->lc; }
+
+/* Work items one CTA takes at a time (warps per CTA with direct painting). */
+extern "C" int32_t fsk_items_per_cta(const FsTune *t) {
+  return t->stage ? 1 : t->tw * t->lc / 32;
 }
 
 /* Level 1 of the max pyramid: each cell is the maximum of the 2x2 texels that

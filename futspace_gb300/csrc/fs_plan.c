@@ -99,6 +99,7 @@ static int plan_enqueue(fs_plan *p) {
 static int plan_build(fs_plan *p) {
   fs_ctx *ctx = p->ctx;
   const int32_t tw = p->tune.tw;
+  const int32_t iw = fsk_item_width(&p->tune);
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   plan_release_graph(p);
@@ -107,8 +108,8 @@ static int plan_build(fs_plan *p) {
     FsView *fv = &p->fv_h[v];
     fv->out = p->frames + p->offsets[v];
     fv->tmap = fs_encode_frame_map(ctx, fv->out, fv->W, fv->H, tw, &p->tm_h[v]) ? v : -1;
-    const int32_t tiles = (fv->W + tw - 1) / tw;
-    if (tiles > 4096) return fs_fail(ctx, FS_ERR_ARG, "view %d: too many column tiles", v);
+    const int32_t tiles = (fv->W + iw - 1) / iw;
+    if (tiles > FS_ITEM_TILES) return fs_fail(ctx, FS_ERR_ARG, "view %d: too many column tiles", v);
     nitems += tiles;
   }
   fs_item_cost *ic = (fs_item_cost *)malloc(sizeof(fs_item_cost) * (size_t)nitems);
@@ -121,10 +122,10 @@ static int plan_build(fs_plan *p) {
   int64_t k = 0;
   for (int v = 0; v < p->nviews; v++) {
     const FsView *fv = &p->fv_h[v];
-    const int32_t tiles = (fv->W + tw - 1) / tw;
+    const int32_t tiles = (fv->W + iw - 1) / iw;
     for (int t = 0; t < tiles; t++) {
       ic[k].cost = (int64_t)fv->n * 8 + fv->H; /* depth march dominates, then the store */
-      ic[k].item = (v << 12) | t;
+      ic[k].item = (v << 16) | t;
       k++;
     }
   }
@@ -150,7 +151,8 @@ static int plan_build(fs_plan *p) {
   if (occ < 1) return fs_fail(ctx, FS_ERR_ARG, "render kernel does not fit on an SM");
   int64_t grid = (int64_t)occ * ctx->sm_count;
   if (p->tune.ctas > 0 && p->tune.ctas < grid) grid = p->tune.ctas;
-  if (grid > nitems) grid = nitems;
+  const int64_t per_cta = fsk_items_per_cta(&p->tune);
+  if (grid > (nitems + per_cta - 1) / per_cta) grid = (nitems + per_cta - 1) / per_cta;
   p->grid = (int32_t)grid;
 
   for (int i = 0; i < 2; i++) {
@@ -203,8 +205,8 @@ int fs_plan_new(fs_ctx *ctx, fs_plan **out, const fs_map *const *maps, int32_t n
   if (ctx->broken) return fs_fail(ctx, FS_ERR_STATE, "context failed to initialise");
   if (!maps || nmaps < 1 || nmaps > FS_MAX_MAPS)
     return fs_fail(ctx, FS_ERR_ARG, "need 1..%d maps", FS_MAX_MAPS);
-  if (!views || nviews < 1 || nviews >= (1 << 19))
-    return fs_fail(ctx, FS_ERR_ARG, "need 1..%d views", (1 << 19) - 1);
+  if (!views || nviews < 1 || nviews >= FS_ITEM_VIEWS)
+    return fs_fail(ctx, FS_ERR_ARG, "need 1..%d views", FS_ITEM_VIEWS - 1);
   for (int i = 0; i < nmaps; i++)
     if (!maps[i]) return fs_fail(ctx, FS_ERR_ARG, "map %d is NULL", i);
   fs_params dp = fs_params_default();

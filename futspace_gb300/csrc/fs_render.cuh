@@ -1,9 +1,12 @@
 /*
  * The voxel-space column renderer (fut/voxel_renderer.fut:214-251, `#off`).
  *
- * Work item = (view, column tile of TW screen columns). One CTA renders an
- * item; with a work counter the CTAs are persistent and pull items until the
- * queue is empty, so views of uneven size and depth share one launch.
+ * Work items: with the shared-memory stage (STG = 1) an item is (view, tile of
+ * TW screen columns) and one CTA renders it; with direct painting (STG = 0)
+ * an item is (view, strip of 32/LC columns) and one warp renders it, with no
+ * CTA barrier between items. With a work counter the CTAs (warps) are
+ * persistent and pull items until the queue is empty, so views of uneven size
+ * and depth share one launch.
  *
  * Lanes: each screen column is marched by LC lanes of a warp (32/LC columns
  * per warp). A chunk covers LC*U consecutive depths; at step u the LC lanes of
@@ -32,9 +35,9 @@
  *           and written with TMA bulk tensor stores (cp.async.bulk.tensor.2d),
  *           32 rows per box, double buffered.
  *  STG = 0: straight into the frame in global memory (tiny shared-memory
- *           footprint, full occupancy); sky rows are written row-wise by the
- *           CTA afterwards, and a column that painted a gap colour gets the gap
- *           fill re-run over its rows.
+ *           footprint, full occupancy); the warp then writes its columns' sky
+ *           rows, a row per store instruction, and re-runs the gap fill over a
+ *           column that painted the gap colour.
  */
 #pragma once
 #include "fs_device.cuh"
@@ -49,7 +52,7 @@ struct QueueCap {
 
 constexpr int kBoxRows = 32;
 
-/* Queue entry: depth index (20 bits) | tile column (7) | row (16) | prev (16). */
+/* Queue entry: depth index (20 bits) | item column (7) | row (16) | prev (16). */
 __device__ __forceinline__ unsigned long long pack_event(int k, int col, int row, int prev) {
   return ((unsigned long long)(uint32_t)k << 39) | ((unsigned long long)(uint32_t)col << 32) |
          ((unsigned long long)(uint32_t)row << 16) | (unsigned long long)(uint32_t)prev;
@@ -112,8 +115,7 @@ struct RenderShape {
   static constexpr size_t box_bytes = STG ? 2ull * kBoxRows * TW * 4 : 0;
   static constexpr size_t queue_bytes = (size_t)NW * QCAP * 8 * QW;
   static constexpr size_t lut_bytes = 256 * 4;
-  static constexpr size_t meta_bytes = (size_t)TW * 8;
-  static constexpr size_t fixed_bytes = box_bytes + queue_bytes + lut_bytes + meta_bytes;
+  static constexpr size_t fixed_bytes = box_bytes + queue_bytes + lut_bytes;
   /* direct painting keeps 64 registers per thread so 32 warps fit per SM:
    * the march is bound by gather latency, and occupancy hides it */
   static constexpr int min_blocks = STG ? 1 : (NT >= 1024 ? 1 : 1024 / NT);
@@ -135,11 +137,270 @@ struct BoolTag {
   static constexpr bool value = B;
 };
 
+/* Per-warp state and work of one item: the march over depth chunks, the event
+ * ring, colouring and painting. Both kernel layouts call it; `cl` is the lane's
+ * column within the item, `c0` the item's first screen column. On return `m`
+ * holds the column's final minimum row and `gapcols` (direct painting) has bit
+ * c set when column c painted the gap colour. */
+template <int TW, int LC, int U, int HF, int CF, int STG, int SM, int FX>
+__device__ __forceinline__ void render_strip(const FsLaunch &P, const FsView *Vp, int c0, int cl,
+                                             int lane, unsigned lanemask_lt,
+                                             unsigned long long *q, uint32_t *stage,
+                                             const LutChannels &chan, int &m_out,
+                                             uint32_t &gapcols, uint32_t &n_samples,
+                                             uint32_t &n_events) {
+  using S = RenderShape<TW, LC, U, STG, SM>;
+  constexpr int CH = LC * U;
+  constexpr int QCAP = S::QCAP;
+  const int dl = lane % LC;
+  /* the view's fields live in registers: the frame stores below may alias
+   * the view records as far as the compiler can tell */
+  const float cam_h = Vp->cam_h, horizon = Vp->horizon;
+  const int W = Vp->W, H = Vp->H, n = Vp->n;
+  const uint32_t sky = Vp->sky, gap = Vp->gap;
+  const int vflags = Vp->flags;
+  const FsMapDev &M = P.maps[Vp->map]; /* read in place: no local copy to index */
+  const HeightMap hmap{M.q, M.MW, M.MH};
+  const bool p2 = M.pow2 != 0;
+  const float4 *zl = P.zline + Vp->zoff;
+  const float *zi = P.zinvz + Vp->zoff;
+  uint32_t *const out = Vp->out;
+  const int stride = H | 1;
+  const int col = c0 + cl;
+  const bool valid = col < W;
+  const float fcol = (float)col;
+
+  /* running minimum row of this column; 0 also marks a column past the
+   * frame's right edge, which never has an event */
+  int m = valid ? H : 0;
+  int qh = 0, qt = 0; /* ring head / tail, warp-uniform */
+  uint32_t gapbits = 0;
+  /* smoothing: the last event of this lane's column, queued once the sample
+   * after it shows whether it held the minimum for a single sample */
+  int pend_k = -1, pend_r = 0, pend_p = 0, pend_kprev = -1;
+
+  /* colour of depth sample k of item column ecl (with the optional epilogue) */
+  auto sample_colour = [&](int k, int ecl) -> uint32_t {
+    const float ec = (float)(c0 + ecl);
+    const float4 L = __ldg(zl + k);
+    const float2 xy = axpy2(ec, make_float2(L.z, L.w), make_float2(L.x, L.y));
+    uint32_t colour = CF ? color_bilinear(M, chan, xy.x, xy.y) : color_nearest(M, xy.x, xy.y);
+    if constexpr (FX) {
+      if (vflags & (FSV_SHADE | FSV_FOG)) {
+        /* depth of sample k, as the depth table computes it */
+        const float fi = (float)(k + 1);
+        const float z = fm(fd(fi, 2.0f), fa(fm(2.0f, Vp->z0), fm(fs(fi, 1.0f), Vp->d)));
+        colour = apply_effects(chan, *Vp, colour, z);
+      }
+    }
+    return colour;
+  };
+
+  /* screen row of depth sample k of this lane's column, clamped to [0, H] */
+  auto sample_row = [&](auto p2tag, int k) -> int {
+    constexpr bool P2 = decltype(p2tag)::value;
+    const float4 L = __ldg(zl + k);
+    const float2 xy = axpy2(fcol, make_float2(L.z, L.w), make_float2(L.x, L.y));
+    const float hh =
+        HF ? height_bilinear<P2>(hmap, xy.x, xy.y) : height_nearest<P2>(hmap, xy.x, xy.y);
+    return min(max(f2i(fa(fm(fs(cam_h, hh), __ldg(zi + k)), horizon)), 0), H);
+  };
+
+  /* colour the queued events [qh, qh+cnt) and paint their intervals */
+  auto drain = [&](int cnt) {
+    uint32_t gb = 0;
+    if (lane < cnt) {
+      const int slot = (qh + lane) & (QCAP - 1);
+      const unsigned long long e = q[slot * S::QW];
+      const int k = (int)(e >> 39);
+      const int ecl = (int)((e >> 32) & 127u);
+      const int er = (int)((e >> 16) & 0xFFFFu);
+      const int ep = (int)(e & 0xFFFFu);
+      const uint32_t colour = sample_colour(k, ecl);
+      if (SM) {
+        const unsigned long long e1 = q[slot * S::QW + S::QW - 1];
+        const int kprev = (int)(e1 & 0x1FFFFFu) - 1; /* previous event, -1: none */
+        const bool blend = ((e1 >> 32) & 1u) != 0;
+        uint32_t cprev = 0u;                         /* the scan's neutral colour */
+        if (blend && kprev >= 0) cprev = sample_colour(kprev, ecl);
+        const float range = fmaxf(1.0f, (float)(ep - er));
+        uint32_t *o = out + (size_t)er * W + c0 + ecl;
+        for (int yy = er; yy < ep; yy++, o += W) {
+          uint32_t c = colour;
+          if (blend) {
+            const float d1 = fd(fabsf(fs((float)yy, (float)ep)), range);
+            const float d2 = fd(fabsf(fs((float)er, (float)yy)), range);
+            c = mix(chan, d2, cprev, d1, colour);
+          }
+          __stcs(o, c == 0u ? sky : c);
+        }
+      } else if (STG) {
+        uint32_t *sc = stage + ecl * stride;
+        for (int yy = er; yy < ep; yy++) sc[yy] = colour;
+      } else {
+        uint32_t *o = out + (size_t)er * W + c0 + ecl;
+        for (int yy = er; yy < ep; yy++, o += W) __stcs(o, colour);
+        if (colour == gap) gb = 1u << ecl;
+      }
+    }
+    if (!STG && !SM) gapbits |= __reduce_or_sync(FS_FULL_MASK, gb);
+    __syncwarp();
+  };
+
+  /* rows of one chunk of depth samples, then its events into the ring */
+  auto march_chunk = [&](auto p2tag, int k0) {
+    int r[U];
+    if constexpr (LC == 1) {
+      /* one lane per column: every lane is at the same depth, so the depth
+       * table loads are uniform and the occlusion test is a plain compare */
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int k = k0 + u;
+        const int rr = sample_row(p2tag, k);
+        r[u] = k < n ? rr : H;
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const bool ev = r[u] < m;
+        if constexpr (SM) {
+          const int k = k0 + u;
+          const bool fin = ev && pend_k >= 0;
+          const unsigned msk = __ballot_sync(FS_FULL_MASK, fin);
+          if (fin) {
+            const int pos = (qt + __popc(msk & lanemask_lt)) & (QCAP - 1);
+            const bool blend = (k == pend_k + 1) &&
+                               (pend_kprev == pend_k - 1 || (pend_kprev < 0 && pend_k == 1));
+            q[pos * S::QW] = pack_event(pend_k, cl, pend_r, pend_p);
+            q[pos * S::QW + S::QW - 1] =
+                (unsigned long long)(uint32_t)(pend_kprev + 1) | ((unsigned long long)blend << 32);
+          }
+          qt += __popc(msk);
+          if (ev) {
+            pend_kprev = pend_k;
+            pend_k = k;
+            pend_r = r[u];
+            pend_p = m;
+          }
+        } else {
+          const unsigned msk = __ballot_sync(FS_FULL_MASK, ev);
+          if (ev) q[(qt + __popc(msk & lanemask_lt)) & (QCAP - 1)] = pack_event(k0 + u, cl, r[u], m);
+          qt += __popc(msk);
+        }
+        m = min(m, r[u]);
+      }
+    } else {
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int k = k0 + u * LC + dl;
+        const int rr = sample_row(p2tag, k);
+        r[u] = k < n ? rr : H;
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        int incl = r[u];
+#pragma unroll
+        for (int off = 1; off < LC; off <<= 1) {
+          const int t = __shfl_up_sync(FS_FULL_MASK, incl, off, LC);
+          if (dl >= off) incl = min(incl, t);
+        }
+        const int excl = __shfl_up_sync(FS_FULL_MASK, incl, 1, LC);
+        const int prev = (dl == 0) ? m : min(m, excl);
+        const bool ev = r[u] < prev;
+        const unsigned msk = __ballot_sync(FS_FULL_MASK, ev);
+        if (ev) {
+          const int pos = (qt + __popc(msk & lanemask_lt)) & (QCAP - 1);
+          q[pos] = pack_event(k0 + u * LC + dl, cl, r[u], prev);
+        }
+        qt += __popc(msk);
+        m = min(m, __shfl_sync(FS_FULL_MASK, incl, LC - 1, LC));
+      }
+    }
+    __syncwarp();
+  };
+
+  /* One loop, one drain site: march a chunk while fewer than 32 events wait,
+   * colour and paint 32 at a time, and flush the rest once the march ends. */
+  int k0 = 0;
+  bool marching = true;
+  for (;;) {
+    if (marching && qt - qh < 32) {
+      if (k0 >= n || __all_sync(FS_FULL_MASK, m == 0)) {
+        marching = false;
+        if constexpr (SM) {
+          /* the column's last event: no later sample is an event, so it held
+           * the minimum for a single sample only if it is the last sample */
+          const bool fin = pend_k >= 0;
+          const unsigned msk = __ballot_sync(FS_FULL_MASK, fin);
+          if (fin) {
+            const int pos = (qt + __popc(msk & lanemask_lt)) & (QCAP - 1);
+            const bool blend = (pend_k == n - 1) &&
+                               (pend_kprev == pend_k - 1 || (pend_kprev < 0 && pend_k == 1));
+            q[pos * S::QW] = pack_event(pend_k, cl, pend_r, pend_p);
+            q[pos * S::QW + S::QW - 1] =
+                (unsigned long long)(uint32_t)(pend_kprev + 1) | ((unsigned long long)blend << 32);
+          }
+          qt += __popc(msk);
+          __syncwarp();
+        }
+      } else {
+        const int kc = k0;
+        k0 += CH;
+        bool skip = false;
+        if (M.pyr) {
+          /* Exact skip: rows are monotone in the height and in inv_z, so a
+           * row computed from an upper bound of every height in the chunk,
+           * at the chunk's nearest or farthest depth, bounds every sample's
+           * row from below. If that bound is not above the running minimum,
+           * no sample of the chunk can be an event for this column. */
+          const int ka = kc, kb = min(kc + CH, n) - 1;
+          bool lskip = m == 0;
+          if (!lskip) {
+            const float4 La = __ldg(zl + ka), Lb = __ldg(zl + kb);
+            const float iza = __ldg(zi + ka), izb = __ldg(zi + kb);
+            const float2 xa = axpy2(fcol, make_float2(La.z, La.w), make_float2(La.x, La.y));
+            const float2 xb = axpy2(fcol, make_float2(Lb.z, Lb.w), make_float2(Lb.x, Lb.y));
+            const float dh =
+                fs(cam_h, fa((float)segment_max_height(M, xa.x, xa.y, xb.x, xb.y), 1.0f));
+            const int ra = min(max(f2i(fa(fm(dh, iza), horizon)), 0), H);
+            const int rb = min(max(f2i(fa(fm(dh, izb), horizon)), 0), H);
+            lskip = min(ra, rb) >= m;
+          }
+          skip = __all_sync(FS_FULL_MASK, lskip);
+        }
+        if (!skip) {
+          if (P.stats && m > 0) {
+            int c = 0;
+#pragma unroll
+            for (int u = 0; u < U; u++) c += (kc + u * LC + dl < n) ? 1 : 0;
+            n_samples += (uint32_t)c;
+          }
+          if (p2)
+            march_chunk(BoolTag<true>{}, kc);
+          else
+            march_chunk(BoolTag<false>{}, kc);
+        }
+      }
+    }
+    const int avail = qt - qh;
+    if (avail >= 32 || (!marching && avail > 0)) {
+      const int cnt = min(avail, 32);
+      drain(cnt);
+      qh += cnt;
+    } else if (!marching) {
+      break;
+    }
+  }
+  n_events += (uint32_t)qt;
+  m_out = m;
+  gapcols = gapbits;
+}
+
 template <int TW, int LC, int U, int HF, int CF, int STG, int SM, int FX>
 __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_blocks))
     render_kernel(const __grid_constant__ FsLaunch P) {
   using S = RenderShape<TW, LC, U, STG, SM>;
   constexpr int NT = S::NT;
+  constexpr int NW = S::NW;
   constexpr int CPW = S::CPW;
   constexpr int CH = LC * U;
   constexpr int QCAP = S::QCAP;
@@ -151,287 +412,54 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
   uint32_t *box = reinterpret_cast<uint32_t *>(smem);
   unsigned long long *queues = reinterpret_cast<unsigned long long *>(smem + S::box_bytes);
   float *lut = reinterpret_cast<float *>(smem + S::box_bytes + S::queue_bytes);
-  int *col_mf = reinterpret_cast<int *>(smem + S::box_bytes + S::queue_bytes + S::lut_bytes);
-  int *col_flag = col_mf + TW;
   uint32_t *stage = reinterpret_cast<uint32_t *>(smem + S::fixed_bytes);
-  __shared__ int s_item;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int dl = lane % LC;
-  const int cl = warp * CPW + lane / LC;
   unsigned long long *q = queues + warp * QCAP * S::QW;
   unsigned lanemask_lt;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lanemask_lt));
   for (int i = tid; i < 256; i += NT) lut[i] = __fdiv_rn((float)i, 255.0f);
+  __syncthreads();
   const LutChannels chan{lut};
   uint32_t n_samples = 0, n_events = 0; /* work counters (ctx stats) */
 
-  for (int iter = 0;; iter++) {
-    int item;
-    if (P.head) {
-      if (tid == 0) s_item = atomicAdd(P.head, 1);
-      if (!STG && tid < TW) col_flag[tid] = 0;
-      __syncthreads();
-      item = s_item;
-    } else {
-      if (!STG && tid < TW) col_flag[tid] = 0;
-      __syncthreads();
-      item = iter == 0 ? (int)blockIdx.x : P.nitems;
-    }
-    if (item >= P.nitems) break;
-    int vi = 0, tile = item;
-    if (P.items) {
-      const int it = P.items[item];
-      vi = it >> 12;
-      tile = it & 4095;
-    }
-    const FsView *Vp = P.views ? P.views + vi : &P.view0;
-    /* the view's fields live in registers: the frame stores below may alias
-     * the view records as far as the compiler can tell */
-    const float cam_h = Vp->cam_h, horizon = Vp->horizon;
-    const int W = Vp->W, H = Vp->H, n = Vp->n;
-    const uint32_t sky = Vp->sky, gap = Vp->gap;
-    const int vflags = Vp->flags;
-    const FsMapDev &M = P.maps[Vp->map]; /* read in place: no local copy to index */
-    const HeightMap hmap{M.q, M.MW, M.MH};
-    const bool p2 = M.pow2 != 0;
-    const float4 *zl = P.zline + Vp->zoff;
-    const float *zi = P.zinvz + Vp->zoff;
-    uint32_t *const out = Vp->out;
-    const int stride = H | 1;
-    const int c0 = tile * TW;
-    const int col = c0 + cl;
-    const bool valid = col < W;
-    const float fcol = (float)col;
-
-    /* running minimum row of this column; 0 also marks a column past the
-     * frame's right edge, which never has an event */
-    int m = valid ? H : 0;
-    int qh = 0, qt = 0; /* ring head / tail, warp-uniform */
-    /* smoothing: the last event of this lane's column, queued once the sample
-     * after it shows whether it held the minimum for a single sample */
-    int pend_k = -1, pend_r = 0, pend_p = 0, pend_kprev = -1;
-
-    /* colour of depth sample k of tile column ecl (with the optional epilogue) */
-    auto sample_colour = [&](int k, int ecl) -> uint32_t {
-      const float ec = (float)(c0 + ecl);
-      const float4 L = __ldg(zl + k);
-      const float2 xy = axpy2(ec, make_float2(L.z, L.w), make_float2(L.x, L.y));
-      uint32_t colour = CF ? color_bilinear(M, chan, xy.x, xy.y) : color_nearest(M, xy.x, xy.y);
-      if constexpr (FX) {
-        if (vflags & (FSV_SHADE | FSV_FOG)) {
-          /* depth of sample k, as the depth table computes it */
-          const float fi = (float)(k + 1);
-          const float z = fm(fd(fi, 2.0f), fa(fm(2.0f, Vp->z0), fm(fs(fi, 1.0f), Vp->d)));
-          colour = apply_effects(chan, *Vp, colour, z);
-        }
-      }
-      return colour;
-    };
-
-    /* screen row of depth sample k of this lane's column, clamped to [0, H] */
-    auto sample_row = [&](auto p2tag, int k) -> int {
-      constexpr bool P2 = decltype(p2tag)::value;
-      const float4 L = __ldg(zl + k);
-      const float2 xy = axpy2(fcol, make_float2(L.z, L.w), make_float2(L.x, L.y));
-      const float hh =
-          HF ? height_bilinear<P2>(hmap, xy.x, xy.y) : height_nearest<P2>(hmap, xy.x, xy.y);
-      return min(max(f2i(fa(fm(fs(cam_h, hh), __ldg(zi + k)), horizon)), 0), H);
-    };
-
-    /* colour the queued events [qh, qh+cnt) and paint their intervals */
-    auto drain = [&](int cnt) {
-      if (lane < cnt) {
-        const int slot = (qh + lane) & (QCAP - 1);
-        const unsigned long long e = q[slot * S::QW];
-        const int k = (int)(e >> 39);
-        const int ecl = (int)((e >> 32) & 127u);
-        const int er = (int)((e >> 16) & 0xFFFFu);
-        const int ep = (int)(e & 0xFFFFu);
-        const uint32_t colour = sample_colour(k, ecl);
-        if (SM) {
-          const unsigned long long e1 = q[slot * S::QW + S::QW - 1];
-          const int kprev = (int)(e1 & 0x1FFFFFu) - 1; /* previous event, -1: none */
-          const bool blend = ((e1 >> 32) & 1u) != 0;
-          uint32_t cprev = 0u;                         /* the scan's neutral colour */
-          if (blend && kprev >= 0) cprev = sample_colour(kprev, ecl);
-          const float range = fmaxf(1.0f, (float)(ep - er));
-          uint32_t *o = out + (size_t)er * W + c0 + ecl;
-          for (int yy = er; yy < ep; yy++, o += W) {
-            uint32_t c = colour;
-            if (blend) {
-              const float d1 = fd(fabsf(fs((float)yy, (float)ep)), range);
-              const float d2 = fd(fabsf(fs((float)er, (float)yy)), range);
-              c = mix(chan, d2, cprev, d1, colour);
-            }
-            __stcs(o, c == 0u ? sky : c);
-          }
-        } else if (STG) {
-          uint32_t *sc = stage + ecl * stride;
-          for (int yy = er; yy < ep; yy++) sc[yy] = colour;
-        } else {
-          uint32_t *o = out + (size_t)er * W + c0 + ecl;
-          for (int yy = er; yy < ep; yy++, o += W) __stcs(o, colour);
-          if (colour == gap) col_flag[ecl] = 1;
-        }
-      }
-      __syncwarp();
-    };
-
-    /* rows of one chunk of depth samples, then its events into the ring */
-    auto march_chunk = [&](auto p2tag, int k0) {
-      int r[U];
-      if constexpr (LC == 1) {
-        /* one lane per column: every lane is at the same depth, so the depth
-         * table loads are uniform and the occlusion test is a plain compare */
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-          const int k = k0 + u;
-          const int rr = sample_row(p2tag, k);
-          r[u] = k < n ? rr : H;
-        }
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-          const bool ev = r[u] < m;
-          if constexpr (SM) {
-            const int k = k0 + u;
-            const bool fin = ev && pend_k >= 0;
-            const unsigned msk = __ballot_sync(FS_FULL_MASK, fin);
-            if (fin) {
-              const int pos = (qt + __popc(msk & lanemask_lt)) & (QCAP - 1);
-              const bool blend = (k == pend_k + 1) &&
-                                 (pend_kprev == pend_k - 1 || (pend_kprev < 0 && pend_k == 1));
-              q[pos * S::QW] = pack_event(pend_k, cl, pend_r, pend_p);
-              q[pos * S::QW + S::QW - 1] =
-                  (unsigned long long)(uint32_t)(pend_kprev + 1) | ((unsigned long long)blend << 32);
-            }
-            qt += __popc(msk);
-            if (ev) {
-              pend_kprev = pend_k;
-              pend_k = k;
-              pend_r = r[u];
-              pend_p = m;
-            }
-          } else {
-            const unsigned msk = __ballot_sync(FS_FULL_MASK, ev);
-            if (ev) q[(qt + __popc(msk & lanemask_lt)) & (QCAP - 1)] = pack_event(k0 + u, cl, r[u], m);
-            qt += __popc(msk);
-          }
-          m = min(m, r[u]);
-        }
+  if constexpr (STG) {
+    /* a CTA per (view, tile of TW columns): march into the column stage,
+     * fill, then transpose and store with TMA */
+    __shared__ int s_item;
+    const int cl = warp * CPW + lane / LC;
+    for (int iter = 0;; iter++) {
+      int item;
+      if (P.head) {
+        if (tid == 0) s_item = atomicAdd(P.head, 1);
+        __syncthreads();
+        item = s_item;
       } else {
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-          const int k = k0 + u * LC + dl;
-          const int rr = sample_row(p2tag, k);
-          r[u] = k < n ? rr : H;
-        }
-#pragma unroll
-        for (int u = 0; u < U; u++) {
-          int incl = r[u];
-#pragma unroll
-          for (int off = 1; off < LC; off <<= 1) {
-            const int t = __shfl_up_sync(FS_FULL_MASK, incl, off, LC);
-            if (dl >= off) incl = min(incl, t);
-          }
-          const int excl = __shfl_up_sync(FS_FULL_MASK, incl, 1, LC);
-          const int prev = (dl == 0) ? m : min(m, excl);
-          const bool ev = r[u] < prev;
-          const unsigned msk = __ballot_sync(FS_FULL_MASK, ev);
-          if (ev) {
-            const int pos = (qt + __popc(msk & lanemask_lt)) & (QCAP - 1);
-            q[pos] = pack_event(k0 + u * LC + dl, cl, r[u], prev);
-          }
-          qt += __popc(msk);
-          m = min(m, __shfl_sync(FS_FULL_MASK, incl, LC - 1, LC));
-        }
+        item = iter == 0 ? (int)blockIdx.x : P.nitems;
       }
-      __syncwarp();
-    };
-
-    /* One loop, one drain site: march a chunk while fewer than 32 events wait,
-     * colour and paint 32 at a time, and flush the rest once the march ends. */
-    int k0 = 0;
-    bool marching = true;
-    for (;;) {
-      if (marching && qt - qh < 32) {
-        if (k0 >= n || __all_sync(FS_FULL_MASK, m == 0)) {
-          marching = false;
-          if constexpr (SM) {
-            /* the column's last event: no later sample is an event, so it held
-             * the minimum for a single sample only if it is the last sample */
-            const bool fin = pend_k >= 0;
-            const unsigned msk = __ballot_sync(FS_FULL_MASK, fin);
-            if (fin) {
-              const int pos = (qt + __popc(msk & lanemask_lt)) & (QCAP - 1);
-              const bool blend = (pend_k == n - 1) &&
-                                 (pend_kprev == pend_k - 1 || (pend_kprev < 0 && pend_k == 1));
-              q[pos * S::QW] = pack_event(pend_k, cl, pend_r, pend_p);
-              q[pos * S::QW + S::QW - 1] =
-                  (unsigned long long)(uint32_t)(pend_kprev + 1) | ((unsigned long long)blend << 32);
-            }
-            qt += __popc(msk);
-            __syncwarp();
-          }
-        } else {
-          const int kc = k0;
-          k0 += CH;
-          bool skip = false;
-          if (M.pyr) {
-            /* Exact skip: rows are monotone in the height and in inv_z, so a
-             * row computed from an upper bound of every height in the chunk,
-             * at the chunk's nearest or farthest depth, bounds every sample's
-             * row from below. If that bound is not above the running minimum,
-             * no sample of the chunk can be an event for this column. */
-            const int ka = kc, kb = min(kc + CH, n) - 1;
-            bool lskip = m == 0;
-            if (!lskip) {
-              const float4 La = __ldg(zl + ka), Lb = __ldg(zl + kb);
-              const float iza = __ldg(zi + ka), izb = __ldg(zi + kb);
-              const float2 xa = axpy2(fcol, make_float2(La.z, La.w), make_float2(La.x, La.y));
-              const float2 xb = axpy2(fcol, make_float2(Lb.z, Lb.w), make_float2(Lb.x, Lb.y));
-              const float dh =
-                  fs(cam_h, fa((float)segment_max_height(M, xa.x, xa.y, xb.x, xb.y), 1.0f));
-              const int ra = min(max(f2i(fa(fm(dh, iza), horizon)), 0), H);
-              const int rb = min(max(f2i(fa(fm(dh, izb), horizon)), 0), H);
-              lskip = min(ra, rb) >= m;
-            }
-            skip = __all_sync(FS_FULL_MASK, lskip);
-          }
-          if (!skip) {
-            if (P.stats && m > 0) {
-              int c = 0;
-#pragma unroll
-              for (int u = 0; u < U; u++) c += (kc + u * LC + dl < n) ? 1 : 0;
-              n_samples += (uint32_t)c;
-            }
-            if (p2)
-              march_chunk(BoolTag<true>{}, kc);
-            else
-              march_chunk(BoolTag<false>{}, kc);
-          }
-        }
+      if (item >= P.nitems) break;
+      int vi = 0, tile = item;
+      if (P.items) {
+        const int it = P.items[item];
+        vi = it >> 16;
+        tile = it & 0xFFFF;
       }
-      const int avail = qt - qh;
-      if (avail >= 32 || (!marching && avail > 0)) {
-        const int cnt = min(avail, 32);
-        drain(cnt);
-        qh += cnt;
-      } else if (!marching) {
-        break;
-      }
-    }
-    n_events += (uint32_t)qt;
-
-    if (STG) {
+      const FsView *Vp = P.views ? P.views + vi : &P.view0;
+      const int c0 = tile * TW;
+      int m;
+      uint32_t gapcols;
+      render_strip<TW, LC, U, HF, CF, STG, SM, FX>(P, Vp, c0, cl, lane, lanemask_lt, q, stage,
+                                                   chan, m, gapcols, n_samples, n_events);
+      const int W = Vp->W, H = Vp->H, stride = H | 1;
+      const uint32_t sky = Vp->sky, gap = Vp->gap;
       /* gap fill + sky for this warp's columns, then the transposed store */
 #pragma unroll 1
       for (int c = 0; c < CPW; c++) {
         const int mf = __shfl_sync(FS_FULL_MASK, m, c * LC);
         const int lcl = warp * CPW + c;
         uint32_t *sc = stage + lcl * stride;
-        if (c0 + lcl < W)
-          fill_column([sc](int y) { return sc + y; }, 0, H, mf, gap, sky, lane);
+        if (c0 + lcl < W) fill_column([sc](int y) { return sc + y; }, 0, H, mf, gap, sky, lane);
       }
       __syncthreads();
       if (Vp->tmap >= 0) {
@@ -457,34 +485,61 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
         }
         if (tid == 0) bulk_wait_read<0>();
       } else {
+        uint32_t *const out = Vp->out;
         for (int e = tid; e < H * TW; e += NT) {
           const int y = e / TW, cc = e - y * TW;
           if (c0 + cc < W) __stcs(out + (size_t)y * W + c0 + cc, stage[cc * stride + y]);
         }
       }
-    } else {
-      /* final minimum rows, gap re-fill of flagged columns, sky rows */
-      if (dl == 0) col_mf[cl] = m;
       __syncthreads();
-#pragma unroll 1
-      for (int c = 0; c < CPW; c++) {
-        const int lcl = warp * CPW + c;
-        if (c0 + lcl < W && col_flag[lcl]) {
-          uint32_t *oc = out + c0 + lcl;
-          const int mf = col_mf[lcl];
-          fill_column([oc, W](int y) { return oc + (size_t)y * W; }, mf, H, mf, gap, sky, lane);
-        }
-      }
-      int top = 0;
-      for (int c = 0; c < TW; c++) top = max(top, col_mf[c]);
-      for (int e = tid; e < top * TW; e += NT) {
-        const int y = e / TW, cc = e - y * TW;
-        if (c0 + cc < W && y < col_mf[cc]) __stcs(out + (size_t)y * W + c0 + cc, sky);
-      }
     }
-    __syncthreads();
+    if (tid == 0) bulk_wait_all();
+  } else {
+    /* a warp per (view, strip of CPW columns): no barrier between items */
+    const int cl = lane / LC;
+    for (int iter = 0;; iter++) {
+      int item;
+      if (P.head) {
+        int got = 0;
+        if (lane == 0) got = atomicAdd(P.head, 1);
+        item = __shfl_sync(FS_FULL_MASK, got, 0);
+      } else {
+        item = iter == 0 ? (int)blockIdx.x * NW + warp : P.nitems;
+      }
+      if (item >= P.nitems) break;
+      int vi = 0, strip = item;
+      if (P.items) {
+        const int it = P.items[item];
+        vi = it >> 16;
+        strip = it & 0xFFFF;
+      }
+      const FsView *Vp = P.views ? P.views + vi : &P.view0;
+      const int c0 = strip * CPW;
+      int m;
+      uint32_t gapcols;
+      render_strip<TW, LC, U, HF, CF, STG, SM, FX>(P, Vp, c0, cl, lane, lanemask_lt, q, stage,
+                                                   chan, m, gapcols, n_samples, n_events);
+      const int W = Vp->W, H = Vp->H;
+      const uint32_t sky = Vp->sky, gap = Vp->gap;
+      uint32_t *const out = Vp->out;
+      /* gap fill over the rows of columns that painted the gap colour */
+      while (gapcols) {
+        const int c = __ffs(gapcols) - 1;
+        gapcols &= gapcols - 1;
+        const int mf = __shfl_sync(FS_FULL_MASK, m, c * LC);
+        uint32_t *oc = out + c0 + c;
+        fill_column([oc, W](int y) { return oc + (size_t)y * W; }, mf, H, mf, gap, sky, lane);
+      }
+      /* sky rows [0, m) of each column: lane (r, c) with c = lane % CPW
+       * writes column c of rows r, r + LC, ... (a row per store for LC = 1) */
+      const int sc = lane % CPW, sr = lane / CPW;
+      const int msc = __shfl_sync(FS_FULL_MASK, m, sc * LC);
+      const int mtop = __reduce_max_sync(FS_FULL_MASK, (unsigned)m);
+      uint32_t *os = out + (size_t)sr * W + c0 + sc;
+      for (int y = sr; y < mtop; y += LC, os += (size_t)LC * W)
+        if (y < msc) __stcs(os, sky);
+    }
   }
-  if (STG && tid == 0) bulk_wait_all();
   if (P.stats) {
     unsigned long long ns = n_samples;
 #pragma unroll

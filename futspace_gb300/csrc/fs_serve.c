@@ -120,6 +120,7 @@ struct fs_server {
   fs_server_config cfg;
   FsTune tune;
   int32_t hf, cf, grid, max_items;
+  int32_t iw; /* screen columns per work item */
   uint8_t *arena_base;
   fs_arena arena;
   FsView *sess_d;
@@ -172,7 +173,7 @@ int fs_server_new(fs_ctx *ctx, fs_server **out, const fs_map *const *maps, int32
   if (ctx->broken) return fs_fail(ctx, FS_ERR_STATE, "context failed to initialise");
   if (!maps || nmaps < 1 || nmaps > FS_MAX_MAPS)
     return fs_fail(ctx, FS_ERR_ARG, "need 1..%d maps", FS_MAX_MAPS);
-  if (cfg->nsessions < 1 || cfg->nsessions >= (1 << 19) || cfg->max_batch < 1 ||
+  if (cfg->nsessions < 1 || cfg->nsessions >= FS_ITEM_VIEWS || cfg->max_batch < 1 ||
       cfg->slots < 1 || cfg->slots > 16 || cfg->max_depths < 1 ||
       cfg->max_depths >= FS_MAX_DEPTHS || cfg->budget_bytes < 256)
     return fs_fail(ctx, FS_ERR_ARG, "bad server configuration");
@@ -221,7 +222,8 @@ int fs_server_new(fs_ctx *ctx, fs_server **out, const fs_map *const *maps, int32
     return fs_fail(ctx, FS_ERR_ARG, "serving needs a compiled direct-paint configuration");
   }
   s->tune = t;
-  s->max_items = cfg->max_batch * ((16384 + t.tw - 1) / t.tw);
+  s->iw = fsk_item_width(&t);
+  s->max_items = cfg->max_batch * ((65536 + s->iw - 1) / s->iw);
   int32_t occ = 0;
   int e = fsk_render_max_ctas_per_sm(&t, s->hf, s->cf, 1, &occ);
   if (e || occ < 1) {
@@ -297,7 +299,7 @@ static int launch_batch(fs_server *s, fs_slot *sl, fs_request *reqs, fs_fifo *re
   while (ready->head < ready->tail && nb < mb) {
     const int32_t ri = ready->q[ready->head % ready->cap];
     fs_request *r = &reqs[ri];
-    const int32_t tiles = (r->width + s->tune.tw - 1) / s->tune.tw;
+    const int32_t tiles = (r->width + s->iw - 1) / s->iw;
     if (ni + tiles > s->max_items) break;
     ready->head++;
     FsView v;
@@ -321,7 +323,7 @@ static int launch_batch(fs_server *s, fs_slot *sl, fs_request *reqs, fs_fifo *re
     ids[nb] = r->session;
     for (int32_t t = 0; t < tiles; t++) {
       scratch[ni].cost = (int64_t)v.n * 8 + v.H;
-      scratch[ni].item = (r->session << 12) | t;
+      scratch[ni].item = (r->session << 16) | t;
       ni++;
     }
     sl->req[nb] = ri;
@@ -355,7 +357,9 @@ static int launch_batch(fs_server *s, fs_slot *sl, fs_request *reqs, fs_fifo *re
     L.stats = ctx->stats_dev;
     L.nitems = ni;
     L.stride_max = 1;
-    const int32_t grid = ni < s->grid ? ni : s->grid;
+    const int32_t per_cta = fsk_items_per_cta(&s->tune);
+    const int32_t need = (ni + per_cta - 1) / per_cta;
+    const int32_t grid = need < s->grid ? need : s->grid;
     e = fsk_render(&L, &s->tune, s->hf, s->cf, grid, sl->st);
     ctx->launches += 2;
   }
