@@ -30,7 +30,7 @@ NEAREST, BILINEAR = 0, 1
 GAP_ZERO, GAP_SKY = 0, 1
 FX_SHADE, FX_FOG = 1, 2
 _ERRORS = {1: "FS_ERR_ARG", 2: "FS_ERR_CUDA", 3: "FS_ERR_RANGE", 4: "FS_ERR_NOMEM",
-           5: "FS_ERR_BUDGET", 6: "FS_ERR_STATE"}
+           5: "FS_ERR_BUDGET", 6: "FS_ERR_STATE", 7: "FS_ERR_IO"}
 
 
 class FsError(RuntimeError):
@@ -183,6 +183,13 @@ def lib():
          [u64, vp, i32, i32, i32, f32, f32, f32, f32, i32, P(Camera)])
     _sig(L, "fsgen_walk", C.c_int,
          [u64, vp, i32, i32, i32, f32, f32, f32, f32, f32, i32, P(Camera)])
+    _sig(L, "fs_png_read", C.c_int, [C.c_char_p, P(vp), P(i64), P(i64)])
+    _sig(L, "fs_png_decode", C.c_int, [vp, C.c_size_t, P(vp), P(i64), P(i64)])
+    _sig(L, "fs_png_write", C.c_int, [C.c_char_p, vp, i64, i64])
+    _sig(L, "fs_data_read", C.c_int, [C.c_char_p, P(vp), C.c_char_p, P(i32), P(i64)])
+    _sig(L, "fs_data_write", C.c_int, [C.c_char_p, vp, C.c_char_p, i32, P(i64)])
+    _sig(L, "fs_free", None, [vp])
+    _sig(L, "fs_map_load_png", C.c_int, [vp, P(vp), C.c_char_p, C.c_char_p])
     _LIB = L
     return L
 
@@ -238,6 +245,69 @@ def gen_cameras(seed: int, heights: np.ndarray, count: int, above=(40.0, 40.0),
     _check(lib().fsgen_cameras(seed, _ptr(h), h.shape[0], h.shape[1], count, above[0], above[1],
                                distance[0], distance[1], screen_h, arr), "fsgen_cameras")
     return list(arr)
+
+
+# ---- map ingest and frame output (PNG, Futhark binary data format) ------------
+
+_DATA_TYPES = {" i32": np.int32, " u32": np.uint32, "  u8": np.uint8, "  i8": np.int8,
+               " f32": np.float32, " i16": np.int16, " u16": np.uint16, " i64": np.int64,
+               " u64": np.uint64, " f64": np.float64, "bool": np.bool_}
+
+
+def _take_u32(p, rows, cols) -> np.ndarray:
+    try:
+        return np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_uint32)),
+                                     shape=(rows, cols)).copy()
+    finally:
+        lib().fs_free(p)
+
+
+def png_read(path) -> np.ndarray:
+    """fs_png_read: a PNG as [rows][cols] u32 0xFFRRGGBB words."""
+    p, r, c = C.c_void_p(), C.c_int64(), C.c_int64()
+    _check(lib().fs_png_read(str(path).encode(), C.byref(p), C.byref(r), C.byref(c)),
+           f"fs_png_read({path})")
+    return _take_u32(p, r.value, c.value)
+
+
+def png_decode(data: bytes) -> np.ndarray:
+    buf = C.create_string_buffer(bytes(data), len(data))
+    p, r, c = C.c_void_p(), C.c_int64(), C.c_int64()
+    _check(lib().fs_png_decode(buf, len(data), C.byref(p), C.byref(r), C.byref(c)),
+           "fs_png_decode")
+    return _take_u32(p, r.value, c.value)
+
+
+def png_write(path, argb: np.ndarray):
+    a = np.ascontiguousarray(argb, np.uint32)
+    assert a.ndim == 2
+    _check(lib().fs_png_write(str(path).encode(), _ptr(a), a.shape[0], a.shape[1]),
+           f"fs_png_write({path})")
+
+
+def data_read(path) -> np.ndarray:
+    """fs_data_read: a value in the Futhark binary data format."""
+    p, t, r = C.c_void_p(), C.create_string_buffer(5), C.c_int32()
+    dims = (C.c_int64 * 8)()
+    _check(lib().fs_data_read(str(path).encode(), C.byref(p), t, C.byref(r), dims),
+           f"fs_data_read({path})")
+    try:
+        dt = np.dtype(_DATA_TYPES[t.value.decode()])
+        shape = tuple(dims[i] for i in range(r.value))
+        n = int(np.prod(shape)) if shape else 1
+        raw = C.string_at(p, n * dt.itemsize) if n else b""
+        return np.frombuffer(raw, dt).reshape(shape).copy()
+    finally:
+        lib().fs_free(p)
+
+
+def data_write(path, array: np.ndarray, type_name: str | None = None):
+    a = np.ascontiguousarray(array)
+    if type_name is None:
+        type_name = {np.dtype(v): k for k, v in _DATA_TYPES.items()}[a.dtype]
+    dims = (C.c_int64 * max(1, a.ndim))(*a.shape)
+    _check(lib().fs_data_write(str(path).encode(), _ptr(a), type_name.encode(), a.ndim, dims),
+           f"fs_data_write({path})")
 
 
 def gen_walk(seed: int, heights: np.ndarray, count: int, step: float = 2.0, yaw: float = 0.02,
@@ -375,6 +445,20 @@ class Map:
                   "fs_map_new")
         self.shape = h.shape
         _LIVE.add(self)
+
+    @classmethod
+    def from_png(cls, ctx: Context, color_png, height_png) -> "Map":
+        """fs_map_load_png: colour and height images as c/interactive.c loads them."""
+        m = cls.__new__(cls)
+        m.ctx = ctx
+        m._h = C.c_void_p()
+        ctx.check(lib().fs_map_load_png(ctx.handle, C.byref(m._h), str(color_png).encode(),
+                                        str(height_png).encode()), "fs_map_load_png")
+        r, c = C.c_int64(), C.c_int64()
+        lib().fs_map_shape(m._h, C.byref(r), C.byref(c))
+        m.shape = (r.value, c.value)
+        _LIVE.add(m)
+        return m
 
     @property
     def handle(self):

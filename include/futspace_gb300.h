@@ -28,6 +28,7 @@ extern "C" {
 #define FS_ERR_NOMEM 4    /* host or device allocation failed */
 #define FS_ERR_BUDGET 5   /* serving: request exceeds the framebuffer budget */
 #define FS_ERR_STATE 6    /* object used in the wrong state */
+#define FS_ERR_IO 7       /* file missing, unreadable or not in the expected format */
 
 /* ---- value types ---------------------------------------------------------- */
 
@@ -300,6 +301,29 @@ int fsgen_cameras(uint64_t seed, const uint8_t *heights, int32_t rows, int32_t c
 int fsgen_walk(uint64_t seed, const uint8_t *heights, int32_t rows, int32_t cols,
                int32_t count, float step, float yaw, float above_lo, float above_hi,
                float distance, int32_t screen_h, fs_camera *out);
+
+/* ---- map ingest and frame output (host) ------------------------------------
+ * PNG images as the reference's front end loads them through FreeImage
+ * (c/freeimage_futspace.h:19-58): 8-bit greyscale, RGB, palette, grey+alpha
+ * or RGBA, not interlaced, to 0xFF000000 | R << 16 | G << 8 | B words, rows top
+ * to bottom. Writing produces an 8-bit RGB PNG (alpha dropped). The Futhark
+ * binary data format is the one tools/png2data.py writes and
+ * tools/data2png.py reads: 'b', version 2, rank, a 4-character element type
+ * such as " i32", " u32" or "  u8", little-endian u64 dimensions, little-endian
+ * elements. Buffers these calls return are released with fs_free. Status:
+ * FS_OK, FS_ERR_ARG, FS_ERR_NOMEM or FS_ERR_IO. */
+int fs_png_read(const char *path, uint32_t **argb, int64_t *rows, int64_t *cols);
+int fs_png_decode(const uint8_t *png, size_t nbytes, uint32_t **argb, int64_t *rows,
+                  int64_t *cols);
+int fs_png_write(const char *path, const uint32_t *argb, int64_t rows, int64_t cols);
+int fs_data_read(const char *path, void **data, char type[5], int32_t *rank, int64_t dims[8]);
+int fs_data_write(const char *path, const void *data, const char *type, int32_t rank,
+                  const int64_t *dims);
+void fs_free(void *p);
+/* A map from a colour PNG and a height PNG of the same size, as
+ * c/interactive.c:43-56 loads data/converted-maps/C<n>W.png and D<n>.png:
+ * heights are the low byte (blue channel) of each height-image word. */
+int fs_map_load_png(fs_ctx *ctx, fs_map **out, const char *color_png, const char *height_png);
 
 #ifdef __cplusplus
 }
