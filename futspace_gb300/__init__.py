@@ -163,6 +163,7 @@ def lib():
     _sig(L, "fs_plan_frame_offset", i64, [vp, i32])
     _sig(L, "fs_plan_total_pixels", i64, [vp])
     _sig(L, "fs_plan_download", C.c_int, [vp, vp])
+    _sig(L, "fs_plan_run_download", C.c_int, [vp, vp, i32])
     _sig(L, "fs_plan_get_tune", C.c_int, [vp, P(i32)])
     _sig(L, "fs_plan_set_tune", C.c_int, [vp, P(i32)])
     _sig(L, "fs_plan_signature", C.c_int, [vp, P(i64)])
@@ -535,6 +536,14 @@ class Plan:
         if out is None:
             out = np.empty(self.total_pixels, np.uint32)
         self.ctx.check(lib().fs_plan_download(self._h, _ptr(out)), "fs_plan_download")
+        return out
+
+    def run_download(self, out: np.ndarray | None = None, groups: int = 4) -> np.ndarray:
+        """fs_plan_run_download: render and copy frames to the host, overlapped."""
+        if out is None:
+            out = np.empty(self.total_pixels, np.uint32)
+        self.ctx.check(lib().fs_plan_run_download(self._h, _ptr(out), groups),
+                       "fs_plan_run_download")
         return out
 
     def frames(self, flat: np.ndarray | None = None) -> list[np.ndarray]:

@@ -40,6 +40,12 @@ void fs_plan_free(fs_plan *p) {
   plan_release_graph(p);
   for (int i = 0; i < 2; i++)
     if (p->ev_render[i]) cudaEventDestroy(p->ev_render[i]);
+  for (int i = 0; i < FS_PLAN_MAX_GROUPS; i++)
+    if (p->grp_done[i]) cudaEventDestroy(p->grp_done[i]);
+  if (p->copy_stream) cudaStreamDestroy(p->copy_stream);
+  cudaFree(p->grp_items_d);
+  cudaFree(p->grp_heads_d);
+  free(p->items_h);
   cudaFree(p->fv_d);
   cudaFree(p->tm_d);
   cudaFree(p->items_d);
@@ -137,7 +143,9 @@ static int plan_build(fs_plan *p) {
   int e = cudaMalloc((void **)&p->items_d, sizeof(int32_t) * (size_t)nitems);
   if (!e) e = cudaMemcpy(p->items_d, items, sizeof(int32_t) * (size_t)nitems,
                          cudaMemcpyHostToDevice);
-  free(items);
+  free(p->items_h);
+  p->items_h = items;
+  p->ngroups = 0; /* group lists follow the items */
   if (e) return fs_cuda_fail(ctx, e, "items upload");
   p->nitems = (int32_t)nitems;
   e = cudaMemcpy(p->fv_d, p->fv_h, sizeof(FsView) * (size_t)p->nviews, cudaMemcpyHostToDevice);
@@ -373,6 +381,91 @@ int fs_plan_download(fs_plan *p, uint32_t *host) {
                           cudaMemcpyDeviceToHost, ctx->stream);
   if (!e) e = cudaStreamSynchronize(ctx->stream);
   if (e) return fs_cuda_fail(ctx, e, "frame download");
+  return FS_OK;
+}
+
+/* Splits the views into `groups` contiguous ranges of about equal pixel count
+ * and uploads each range's items (in launch order) with its own work counter. */
+static int plan_build_groups(fs_plan *p, int32_t groups) {
+  fs_ctx *ctx = p->ctx;
+  int64_t done_px = 0, v = 0;
+  p->grp_first[0] = 0;
+  for (int g = 0; g < groups; g++) {
+    const int64_t target = p->total_px * (g + 1) / groups;
+    const int64_t left = groups - g - 1; /* keep a view for every later group */
+    while (v < p->nviews - left && (done_px < target || v == p->grp_first[g])) {
+      done_px += (int64_t)p->fv_h[v].W * p->fv_h[v].H;
+      v++;
+    }
+    p->grp_first[g + 1] = (int32_t)v;
+  }
+  p->grp_first[groups] = p->nviews;
+  int32_t *sorted = (int32_t *)malloc(sizeof(int32_t) * (size_t)p->nitems);
+  if (!sorted) return fs_fail(ctx, FS_ERR_NOMEM, "malloc(group items)");
+  int32_t k = 0;
+  for (int g = 0; g < groups; g++) {
+    p->grp_item_off[g] = k;
+    for (int32_t i = 0; i < p->nitems; i++) {
+      const int32_t view = p->items_h[i] >> 16;
+      if (view >= p->grp_first[g] && view < p->grp_first[g + 1]) sorted[k++] = p->items_h[i];
+    }
+  }
+  p->grp_item_off[groups] = k;
+  cudaFree(p->grp_items_d);
+  p->grp_items_d = NULL;
+  int e = cudaMalloc((void **)&p->grp_items_d, sizeof(int32_t) * (size_t)(k ? k : 1));
+  if (!e) e = cudaMemcpy(p->grp_items_d, sorted, sizeof(int32_t) * (size_t)k, cudaMemcpyHostToDevice);
+  free(sorted);
+  if (!e && !p->grp_heads_d)
+    e = cudaMalloc((void **)&p->grp_heads_d, sizeof(int32_t) * FS_PLAN_MAX_GROUPS);
+  if (!e && !p->copy_stream) e = cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking);
+  for (int g = 0; !e && g < FS_PLAN_MAX_GROUPS; g++)
+    if (!p->grp_done[g]) e = cudaEventCreateWithFlags(&p->grp_done[g], cudaEventDisableTiming);
+  if (e) return fs_cuda_fail(ctx, e, "group set-up");
+  p->ngroups = groups;
+  return FS_OK;
+}
+
+int fs_plan_run_download(fs_plan *p, uint32_t *host, int32_t groups) {
+  if (!p || !host) return FS_ERR_ARG;
+  fs_ctx *ctx = p->ctx;
+  if (!p->graph_ok) return fs_fail(ctx, FS_ERR_STATE, "plan has no kernel configuration");
+  if (groups < 1) groups = 1;
+  if (groups > FS_PLAN_MAX_GROUPS) groups = FS_PLAN_MAX_GROUPS;
+  if (groups > p->nviews) groups = p->nviews;
+  cudaSetDevice(ctx->device);
+  int rc = FS_OK;
+  if (p->ngroups != groups) {
+    cudaStreamSynchronize(ctx->stream);
+    rc = plan_build_groups(p, groups);
+    if (rc) return rc;
+  }
+  int32_t max_n = 0;
+  for (int v = 0; v < p->nviews; v++)
+    if (p->ncap[v] > max_n) max_n = p->ncap[v];
+  int e = cudaMemsetAsync(p->grp_heads_d, 0, sizeof(int32_t) * (size_t)groups, ctx->stream);
+  if (!e) e = fsk_ztable(p->fv_d, NULL, p->nviews, max_n, p->zline, p->zinvz, ctx->stream);
+  const int32_t per_cta = fsk_items_per_cta(&p->tune);
+  for (int g = 0; !e && g < groups; g++) {
+    FsLaunch L;
+    plan_fill_launch(p, &L);
+    L.items = p->grp_items_d + p->grp_item_off[g];
+    L.nitems = p->grp_item_off[g + 1] - p->grp_item_off[g];
+    L.head = p->grp_heads_d + g;
+    int32_t grid = (L.nitems + per_cta - 1) / per_cta;
+    if (grid > p->grid) grid = p->grid;
+    if (L.nitems > 0) e = fsk_render(&L, &p->tune, p->hf, p->cf, grid, ctx->stream);
+    if (!e) e = cudaEventRecord(p->grp_done[g], ctx->stream);
+    if (!e) e = cudaStreamWaitEvent(p->copy_stream, p->grp_done[g], 0);
+    const int64_t a = p->offsets[p->grp_first[g]];
+    const int64_t b = p->grp_first[g + 1] < p->nviews ? p->offsets[p->grp_first[g + 1]] : p->total_px;
+    if (!e && b > a)
+      e = cudaMemcpyAsync(host + a, p->frames + a, sizeof(uint32_t) * (size_t)(b - a),
+                          cudaMemcpyDeviceToHost, p->copy_stream);
+  }
+  ctx->launches += 1 + groups;
+  if (!e) e = cudaStreamSynchronize(p->copy_stream);
+  if (e) return fs_cuda_fail(ctx, e, "pipelined render and download");
   return FS_OK;
 }
 

@@ -52,6 +52,8 @@ struct fs_map {
   int64_t rows, cols;
 };
 
+#define FS_PLAN_MAX_GROUPS 16
+
 struct fs_plan {
   fs_ctx *ctx;
   int32_t nviews, nmaps;
@@ -80,6 +82,17 @@ struct fs_plan {
   cudaGraphExec_t exec;
   int32_t graph_ok;
   cudaEvent_t ev_render[2]; /* recorded around the render kernel inside the graph */
+  int32_t *items_h;          /* the items in launch order (host copy) */
+  /* pipelined render + download (fs_plan_run_download): views split into
+   * contiguous groups, each rendered by its own launch while earlier groups'
+   * frames are copied to the host on copy_stream */
+  int32_t ngroups; /* 0: not built for the current items */
+  int32_t grp_first[FS_PLAN_MAX_GROUPS + 1];
+  int32_t grp_item_off[FS_PLAN_MAX_GROUPS + 1];
+  int32_t *grp_items_d;
+  int32_t *grp_heads_d;
+  cudaStream_t copy_stream;
+  cudaEvent_t grp_done[FS_PLAN_MAX_GROUPS];
 };
 
 int fs_fail(fs_ctx *ctx, int code, const char *fmt, ...);

@@ -99,6 +99,14 @@ def test_batch_plan_all_configurations(fs, orc, gpu_ctx, maps1024):
         assert not bad, (tune, bad)
     plan.run_per_view()
     assert all(count_diff(f, r) == 0 for f, r in zip(plan.frames(), refs))
+    # pipelined render + download: same frames for any grouping, after a
+    # tuning change too (the group lists follow the items)
+    buf = fs.PinnedBuffer(plan.total_pixels)
+    for groups in (1, 3, 16):
+        flat = plan.run_download(buf.array, groups=groups)
+        bad = [i for i, (f, r) in enumerate(zip(plan.frames(flat), refs)) if count_diff(f, r)]
+        assert not bad, (groups, bad)
+        plan.set_tune(*fs.tune_table()[groups % len(fs.tune_table())])
 
 
 def test_batch_two_maps_and_camera_update(fs, orc, gpu_ctx, maps1024, maps256):
