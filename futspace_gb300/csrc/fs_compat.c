@@ -562,7 +562,7 @@ int futhark_entry_render(struct futhark_context *ctx, struct futhark_u32_2d **ou
   M.pow2 = ((M.MH & (M.MH - 1)) == 0) && ((M.MW & (M.MW - 1)) == 0);
   M.cpow2 = ((M.CH & (M.CH - 1)) == 0) && ((M.CW & (M.CW - 1)) == 0);
   v.out = a->dev;
-  rc = fs_render_view(ctx->fs, &M, &v, NULL, ctx->fs->zline, ctx->fs->zinvz, NULL);
+  rc = fs_render_view(ctx->fs, &M, &v, NULL, ctx->fs->zline, ctx->fs->zinvz, NULL, 1);
   if (rc) {
     futhark_free_u32_2d(ctx, a);
     return rc;

@@ -139,6 +139,8 @@ int fs_make_view(fs_ctx *ctx, const fs_camera *cam, const fs_params *p, int32_t 
   v->fog_start = p->fog_start;
   v->fog_end = p->fog_end;
   v->fog_color = p->fog_color;
+  v->nseg = 1;
+  v->seglen = n;
   return FS_OK;
 }
 
@@ -200,6 +202,7 @@ void fs_ctx_free(fs_ctx *ctx) {
   cudaFree(ctx->zline);
   cudaFree(ctx->zinvz);
   cudaFree(ctx->frame_dev);
+  cudaFree(ctx->segbuf);
   cudaFree(ctx->stats_dev);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   free(ctx);
@@ -229,6 +232,8 @@ int fs_ctx_set_option(fs_ctx *ctx, const char *name, int64_t value) {
     ctx->no_skip = value ? 0 : 1;
   } else if (!strcmp(name, "tma")) {
     ctx->use_tma = (value && ctx->encode) ? 1 : 0;
+  } else if (!strcmp(name, "split")) {
+    ctx->no_split = value ? 0 : 1;
   } else {
     return fs_fail(ctx, FS_ERR_ARG, "unknown option '%s'", name);
   }
@@ -515,8 +520,40 @@ FsTune fs_default_tune(fs_ctx *ctx, int32_t stride_max) {
 
 /* ---- plain per-frame render ------------------------------------------------------ */
 
+/* Depth segments per view for direct painting: enough (view, segment, strip)
+ * items for two per resident warp, given `strips` strips in the launch. A
+ * segment keeps at least 4 chunks (split_segments caps it per view). */
+int32_t fs_split_target(fs_ctx *ctx, const FsTune *t, int32_t hf, int32_t cf, int32_t stride,
+                        int64_t strips) {
+  if (ctx->no_split || t->stage || t->smooth || t->fx || strips <= 0) return 1;
+  int32_t occ = 0;
+  if (fsk_render_max_ctas_per_sm(t, hf, cf, stride, &occ) || occ < 1) return 1;
+  const int64_t warps = (int64_t)occ * ctx->sm_count * fsk_items_per_cta(t);
+  int64_t nseg = (2 * warps + strips - 1) / strips;
+  if (nseg < 1) nseg = 1;
+  if (nseg > FS_MAX_SEGMENTS) nseg = FS_MAX_SEGMENTS;
+  return (int32_t)nseg;
+}
+
+/* Splits v's n depths into at most nseg segments of a whole number of
+ * `chunk`-depth chunks, at least 4 chunks each. */
+void fs_set_segments(FsView *v, int32_t nseg, int32_t chunk) {
+  const int32_t most = v->n / (4 * chunk);
+  if (nseg > most) nseg = most;
+  if (nseg <= 1) {
+    v->nseg = 1;
+    v->seglen = v->n;
+    return;
+  }
+  int32_t seglen = (v->n + nseg - 1) / nseg;
+  seglen = (seglen + chunk - 1) / chunk * chunk;
+  v->seglen = seglen;
+  v->nseg = (v->n + seglen - 1) / seglen;
+}
+
 int fs_render_view(fs_ctx *ctx, const FsMapDev *map, FsView *v, const FsTune *tune_in,
-                   float4 *zline, float *zinvz, const CUtensorMap *tmap_pre) {
+                   float4 *zline, float *zinvz, const CUtensorMap *tmap_pre,
+                   int32_t allow_split) {
   const int32_t stride = v->H | 1;
   FsTune t;
   if (tune_in && tune_in->tw) t = *tune_in;
@@ -526,6 +563,28 @@ int fs_render_view(fs_ctx *ctx, const FsMapDev *map, FsView *v, const FsTune *tu
   t = fs_tune_for_mode(t, v->flags);
   if (!t.tw || !fs_tune_fits(ctx, &t, stride))
     return fs_fail(ctx, FS_ERR_ARG, "no kernel configuration fits screen height %d", v->H);
+  const int32_t hf = (v->flags & FSV_HEIGHT_BILINEAR) != 0;
+  const int32_t cf = (v->flags & FSV_COLOR_BILINEAR) != 0;
+  const int32_t iw = fsk_item_width(&t), ntiles = (v->W + iw - 1) / iw;
+  const int32_t per_cta = fsk_items_per_cta(&t);
+  /* a frame with few strips splits each column's depths over several warps */
+  fs_set_segments(v, allow_split ? fs_split_target(ctx, &t, hf, cf, stride, ntiles) : 1,
+                  t.lc * t.u);
+  v->segbuf = NULL;
+  t.seg = v->nseg > 1;
+  if (v->nseg > 1) {
+    const int64_t need = (int64_t)(v->nseg + 2) * v->W;
+    if (need > ctx->segcap) {
+      cudaStreamSynchronize(ctx->stream);
+      cudaFree(ctx->segbuf);
+      ctx->segbuf = NULL;
+      ctx->segcap = 0;
+      if (cudaMalloc((void **)&ctx->segbuf, sizeof(int32_t) * (size_t)need) != cudaSuccess)
+        return fs_fail(ctx, FS_ERR_NOMEM, "cudaMalloc(segment rows)");
+      ctx->segcap = need;
+    }
+    v->segbuf = ctx->segbuf;
+  }
   FsLaunch launch;
   FsLaunch *L = &launch;
   memset(L, 0, sizeof(*L));
@@ -542,16 +601,27 @@ int fs_render_view(fs_ctx *ctx, const FsMapDev *map, FsView *v, const FsTune *tu
   L->zline = zline;
   L->zinvz = zinvz;
   L->stats = ctx->stats_dev;
-  L->nitems = (v->W + fsk_item_width(&t) - 1) / fsk_item_width(&t);
+  L->nitems = ntiles * v->nseg;
   L->stride_max = stride;
-  const int32_t per_cta = fsk_items_per_cta(&t);
   int e = fsk_ztable(NULL, &L->view0, 1, v->n, zline, zinvz, ctx->stream);
   if (e) return fs_cuda_fail(ctx, e, "z-table kernel launch");
-  e = fsk_render(L, &t, (v->flags & FSV_HEIGHT_BILINEAR) != 0,
-                 (v->flags & FSV_COLOR_BILINEAR) != 0, (L->nitems + per_cta - 1) / per_cta,
-                 ctx->stream);
+  if (v->nseg > 1) {
+    /* minimum row of every segment but the last, before the render pass */
+    FsLaunch A = *L;
+    A.stats = NULL;
+    A.nitems = ntiles * (v->nseg - 1);
+    e = fsk_segmin(&A, &t, hf, (A.nitems + per_cta - 1) / per_cta, ctx->stream);
+    if (e) return fs_cuda_fail(ctx, e, "segment-minimum kernel launch");
+    ctx->launches++;
+  }
+  e = fsk_render(L, &t, hf, cf, (L->nitems + per_cta - 1) / per_cta, ctx->stream);
   if (e) return fs_cuda_fail(ctx, e, "render kernel launch");
   ctx->launches += 2;
+  if (v->nseg > 1) {
+    e = fsk_gapfill(NULL, &L->view0, 1, v->W, ctx->stream);
+    if (e) return fs_cuda_fail(ctx, e, "gap-fill kernel launch");
+    ctx->launches++;
+  }
   return FS_OK;
 }
 
@@ -569,7 +639,7 @@ int fs_render_device(fs_ctx *ctx, const fs_map *map, const fs_camera *cam,
   rc = fs_ensure_ztable(ctx, v.n);
   if (rc) return rc;
   v.out = out_dev;
-  return fs_render_view(ctx, &map->dev, &v, NULL, ctx->zline, ctx->zinvz, NULL);
+  return fs_render_view(ctx, &map->dev, &v, NULL, ctx->zline, ctx->zinvz, NULL, 1);
 }
 
 int fs_render(fs_ctx *ctx, const fs_map *map, const fs_camera *cam, const fs_params *params,

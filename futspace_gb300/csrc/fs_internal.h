@@ -53,7 +53,14 @@ typedef struct {
   float distance;   /* draw distance D (depth shading) */
   float shade, fog_start, fog_end;
   uint32_t fog_color;
-  int32_t pad[5];
+  /* depth segments (direct painting only): the column's depth schedule split
+   * into nseg ranges of seglen samples, each marched by its own work item;
+   * segbuf holds [nseg + 2][W] ints: the minimum row of each segment but the
+   * last, the column's final minimum row, and gap-colour flags */
+  int32_t nseg;
+  int32_t *segbuf;
+  int32_t seglen;
+  int32_t pad1;
 } FsView;
 
 /* One height/colour map pair resident in device memory. Heights are stored as
@@ -83,7 +90,8 @@ typedef struct {
   FsView view0;                /* the view when views == NULL */
   FsMapDev maps[FS_MAX_MAPS];
   const FsView *views;         /* NULL: single view0 */
-  const int32_t *items;        /* work items, (view << 12) | tile; NULL: item = tile of view0 */
+  const int64_t *items;        /* work items (FS_ITEM); NULL: item i of view0 is segment
+                                * i / ntiles, tile i % ntiles */
   const CUtensorMap *tmaps;    /* tensor maps of `views` */
   const float4 *zline;         /* per depth: x0, y0, dx, dy */
   const float *zinvz;          /* per depth: inv_z */
@@ -103,6 +111,7 @@ typedef struct {
   int32_t ctas;  /* persistent CTAs (0: as many as fit) */
   int32_t smooth; /* 1: the `#on` smoothing kernels (FS_TUNE_LIST_SM) */
   int32_t fx;     /* 1: kernels with the shading / fog epilogue compiled in */
+  int32_t seg;    /* 1: kernels that read depth segments (some view is split) */
 } FsTune;
 
 /* Kernel-side entry points (fs_kernels.cu). Each returns a cudaError_t. */
@@ -117,10 +126,19 @@ int fsk_render_max_ctas_per_sm(const FsTune *t, int32_t hf, int32_t cf, int32_t 
                                int32_t *out);
 int fsk_tune_supported(const FsTune *t);
 int32_t fsk_item_width(const FsTune *t);
+int fsk_segmin(const FsLaunch *L, const FsTune *t, int32_t hf, int32_t grid, cudaStream_t st);
+int fsk_gapfill(const FsView *views_dev, const FsView *view0, int32_t nviews, int32_t max_w,
+                cudaStream_t st);
 int32_t fsk_items_per_cta(const FsTune *t);
-/* Work items pack (view or session << 16) | column tile or strip. */
+/* A work item names a view (or serving session), a depth segment and a column
+ * tile (shared-memory stage) or strip (direct painting). */
 #define FS_ITEM_VIEWS 32768
 #define FS_ITEM_TILES 65536
+#define FS_MAX_SEGMENTS 32
+#define FS_ITEM(view, seg, tile) (((int64_t)(view) << 40) | ((int64_t)(seg) << 32) | (int64_t)(tile))
+#define FS_ITEM_VIEW(it) ((int32_t)((it) >> 40))
+#define FS_ITEM_SEG(it) ((int32_t)(((it) >> 32) & 0xFF))
+#define FS_ITEM_TILE(it) ((int32_t)((it)&0xFFFFFFFF))
 int fsk_shadowmap(const FsMapDev *map, const float sun[3], uint32_t *out, cudaStream_t st);
 int fsk_mask_heights(const int32_t *in, uint8_t *out, int64_t count, cudaStream_t st);
 int fsk_build_quads(const uint8_t *h, uint32_t *q, int32_t MH, int32_t MW, cudaStream_t st);

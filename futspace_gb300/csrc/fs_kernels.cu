@@ -22,6 +22,8 @@ extern "C" int fsk_render_h1c0(int, const FsLaunch *, const FsTune *, int, size_
                                int *);
 extern "C" int fsk_render_h1c1(int, const FsLaunch *, const FsTune *, int, size_t, cudaStream_t,
                                int *);
+extern "C" int fsk_segmin_h0(const FsLaunch *, const FsTune *, int, cudaStream_t);
+extern "C" int fsk_segmin_h1(const FsLaunch *, const FsTune *, int, cudaStream_t);
 
 namespace {
 
@@ -122,6 +124,22 @@ typedef int (*render_entry)(int, const FsLaunch *, const FsTune *, int, size_t, 
 render_entry pick(int hf, int cf) {
   if (hf) return cf ? fsk_render_h1c1 : fsk_render_h1c0;
   return cf ? fsk_render_h0c1 : fsk_render_h0c0;
+}
+
+/* Gap-fill pass of split views: the reference's forward fill over the rows of
+ * every column a segment flagged for painting the gap colour. A warp per
+ * column; blockIdx.y is the view. */
+__global__ void gapfill_kernel(const FsView *views, FsView view0) {
+  const FsView *Vp = views ? views + blockIdx.y : &view0;
+  if (Vp->nseg <= 1) return;
+  const int lane = threadIdx.x & 31;
+  const int col = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int W = Vp->W, nseg = Vp->nseg;
+  if (col >= W || !Vp->segbuf[(size_t)(nseg + 1) * W + col]) return;
+  const int mf = Vp->segbuf[(size_t)nseg * W + col];
+  uint32_t *oc = Vp->out + col;
+  fill_column([oc, W](int y) { return oc + (size_t)y * W; }, mf, Vp->H, mf, Vp->gap, Vp->sky,
+              lane);
 }
 
 }  // namespace
@@ -244,6 +262,23 @@ extern "C" int fsk_render(const FsLaunch *L, const FsTune *t, int32_t hf, int32_
                           int32_t grid, cudaStream_t st) {
   if (grid <= 0) return (int)cudaSuccess;
   return pick(hf, cf)(0, L, t, grid, fsk_render_smem(t, L->stride_max), st, nullptr);
+}
+
+extern "C" int fsk_gapfill(const FsView *views_dev, const FsView *view0, int32_t nviews,
+                           int32_t max_w, cudaStream_t st) {
+  if (nviews <= 0 || max_w <= 0) return (int)cudaSuccess;
+  FsView v0;
+  if (view0) v0 = *view0;
+  else memset(&v0, 0, sizeof(v0));
+  dim3 grid((max_w + 7) / 8, views_dev ? nviews : 1);
+  gapfill_kernel<<<grid, 256, 0, st>>>(views_dev, v0);
+  return (int)cudaGetLastError();
+}
+
+extern "C" int fsk_segmin(const FsLaunch *L, const FsTune *t, int32_t hf, int32_t grid,
+                          cudaStream_t st) {
+  if (grid <= 0) return (int)cudaSuccess;
+  return (hf ? fsk_segmin_h1 : fsk_segmin_h0)(L, t, grid, st);
 }
 
 extern "C" int fsk_render_max_ctas_per_sm(const FsTune *t, int32_t hf, int32_t cf,

@@ -79,5 +79,5 @@ extern "C" int fs_render_device_noalloc(fs_ctx *ctx, const fs_map *map, const fs
   float *zinvz = reinterpret_cast<float *>(static_cast<unsigned char *>(scratch) +
                                            sizeof(float4) * FS_NOALLOC_ENTRIES);
   v.out = out_dev;
-  return fs_render_view(ctx, &map->dev, &v, nullptr, zline, zinvz, nullptr);
+  return fs_render_view(ctx, &map->dev, &v, nullptr, zline, zinvz, nullptr, 0);
 }

@@ -16,7 +16,7 @@
 
 typedef struct {
   int64_t cost;
-  int32_t item;
+  int64_t item;
 } fs_item_cost;
 
 static int cmp_cost_desc(const void *a, const void *b) {
@@ -50,6 +50,8 @@ void fs_plan_free(fs_plan *p) {
   cudaFree(p->tm_d);
   cudaFree(p->items_d);
   cudaFree(p->head_d);
+  cudaFree(p->segitems_d);
+  cudaFree(p->segbuf_d);
   cudaFree(p->zline);
   cudaFree(p->zinvz);
   cudaFree(p->frames);
@@ -78,25 +80,55 @@ static void plan_fill_launch(fs_plan *p, FsLaunch *L) {
   L->stats = p->ctx->stats_dev;
 }
 
+/* The segment-minimum pass over every split view (none when nothing is split). */
+static int plan_segmin(fs_plan *p) {
+  if (!p->nsegitems) return 0;
+  FsLaunch L;
+  plan_fill_launch(p, &L);
+  L.items = p->segitems_d;
+  L.nitems = p->nsegitems;
+  L.head = p->head_d + 1;
+  L.stats = NULL;
+  const int32_t per_cta = fsk_items_per_cta(&p->tune);
+  int32_t grid = (p->nsegitems + per_cta - 1) / per_cta;
+  if (grid > p->grid) grid = p->grid;
+  return fsk_segmin(&L, &p->tune, p->hf, grid, p->ctx->stream);
+}
+
+/* The render kernel's configuration with the segment-reading variant when some
+ * view is split. */
+static FsTune plan_kernel_tune(const fs_plan *p) {
+  FsTune t = p->tune;
+  t.seg = p->segbuf_d != NULL;
+  return t;
+}
+
 static int plan_enqueue(fs_plan *p) {
   fs_ctx *ctx = p->ctx;
+  const FsTune kt = plan_kernel_tune(p);
   FsLaunch launch;
   plan_fill_launch(p, &launch);
   int32_t max_n = 0;
   for (int v = 0; v < p->nviews; v++)
     if (p->ncap[v] > max_n) max_n = p->ncap[v];
-  int e = cudaMemsetAsync(p->head_d, 0, sizeof(int32_t), ctx->stream);
+  int e = cudaMemsetAsync(p->head_d, 0, 2 * sizeof(int32_t), ctx->stream);
   if (e) return fs_cuda_fail(ctx, e, "work counter reset");
   e = fsk_ztable(p->fv_d, NULL, p->nviews, max_n, p->zline, p->zinvz, ctx->stream);
   if (e) return fs_cuda_fail(ctx, e, "z-table kernel launch");
+  e = plan_segmin(p);
+  if (e) return fs_cuda_fail(ctx, e, "segment-minimum kernel launch");
   /* external event nodes bracket the render kernel, so its device time is
    * readable after every replay of the graph */
   e = cudaEventRecordWithFlags(p->ev_render[0], ctx->stream, cudaEventRecordExternal);
   if (e) return fs_cuda_fail(ctx, e, "render start event");
-  e = fsk_render(&launch, &p->tune, p->hf, p->cf, p->grid, ctx->stream);
+  e = fsk_render(&launch, &kt, p->hf, p->cf, p->grid, ctx->stream);
   if (e) return fs_cuda_fail(ctx, e, "persistent render kernel launch");
   e = cudaEventRecordWithFlags(p->ev_render[1], ctx->stream, cudaEventRecordExternal);
   if (e) return fs_cuda_fail(ctx, e, "render end event");
+  if (p->segbuf_d) {
+    e = fsk_gapfill(p->fv_d, NULL, p->nviews, p->wmax, ctx->stream);
+    if (e) return fs_cuda_fail(ctx, e, "gap-fill kernel launch");
+  }
   return FS_OK;
 }
 
@@ -106,33 +138,69 @@ static int plan_build(fs_plan *p) {
   fs_ctx *ctx = p->ctx;
   const int32_t tw = p->tune.tw;
   const int32_t iw = fsk_item_width(&p->tune);
+  const int32_t chunk = p->tune.lc * p->tune.u;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   plan_release_graph(p);
-  int64_t nitems = 0;
+  int32_t occ = 0;
+  int e = fsk_render_max_ctas_per_sm(&p->tune, p->hf, p->cf, p->stride_max, &occ);
+  if (e) return fs_cuda_fail(ctx, e, "occupancy query");
+  if (occ < 1) return fs_fail(ctx, FS_ERR_ARG, "render kernel does not fit on an SM");
+  /* few strips in the whole batch: split every column's depths into segments */
+  int64_t strips = 0;
+  for (int v = 0; v < p->nviews; v++) strips += (p->fv_h[v].W + iw - 1) / iw;
+  const int32_t target = fs_split_target(ctx, &p->tune, p->hf, p->cf, p->stride_max, strips);
+  int64_t nitems = 0, nseg_items = 0, seg_rows = 0;
   for (int v = 0; v < p->nviews; v++) {
     FsView *fv = &p->fv_h[v];
     fv->out = p->frames + p->offsets[v];
     fv->tmap = fs_encode_frame_map(ctx, fv->out, fv->W, fv->H, tw, &p->tm_h[v]) ? v : -1;
     const int32_t tiles = (fv->W + iw - 1) / iw;
     if (tiles > FS_ITEM_TILES) return fs_fail(ctx, FS_ERR_ARG, "view %d: too many column tiles", v);
-    nitems += tiles;
+    /* segments from the depth count the plan was built with; a later shorter
+     * draw distance leaves trailing segments empty */
+    const int32_t n_now = fv->n;
+    fv->n = p->ncap[v];
+    fs_set_segments(fv, target, chunk);
+    fv->n = n_now;
+    nitems += (int64_t)tiles * fv->nseg;
+    if (fv->nseg > 1) {
+      nseg_items += (int64_t)tiles * (fv->nseg - 1);
+      seg_rows += (int64_t)(fv->nseg + 2) * fv->W;
+    }
+  }
+  cudaFree(p->segbuf_d);
+  p->segbuf_d = NULL;
+  if (seg_rows) {
+    e = cudaMalloc((void **)&p->segbuf_d, sizeof(int32_t) * (size_t)seg_rows);
+    if (e) return fs_cuda_fail(ctx, e, "cudaMalloc(segment rows)");
   }
   fs_item_cost *ic = (fs_item_cost *)malloc(sizeof(fs_item_cost) * (size_t)nitems);
-  int32_t *items = (int32_t *)malloc(sizeof(int32_t) * (size_t)nitems);
-  if (!ic || !items) {
+  int64_t *items = (int64_t *)malloc(sizeof(int64_t) * (size_t)nitems);
+  int64_t *segitems = (int64_t *)malloc(sizeof(int64_t) * (size_t)(nseg_items ? nseg_items : 1));
+  if (!ic || !items || !segitems) {
     free(ic);
     free(items);
+    free(segitems);
     return fs_fail(ctx, FS_ERR_NOMEM, "malloc(items)");
   }
-  int64_t k = 0;
+  int64_t k = 0, ks = 0, row_off = 0;
   for (int v = 0; v < p->nviews; v++) {
-    const FsView *fv = &p->fv_h[v];
+    FsView *fv = &p->fv_h[v];
+    fv->segbuf = NULL;
+    if (fv->nseg > 1) {
+      fv->segbuf = p->segbuf_d + row_off;
+      row_off += (int64_t)(fv->nseg + 2) * fv->W;
+    }
     const int32_t tiles = (fv->W + iw - 1) / iw;
-    for (int t = 0; t < tiles; t++) {
-      ic[k].cost = (int64_t)fv->n * 8 + fv->H; /* depth march dominates, then the store */
-      ic[k].item = (v << 16) | t;
-      k++;
+    for (int s = 0; s < fv->nseg; s++) {
+      for (int t = 0; t < tiles; t++) {
+        /* depth march dominates, then the store */
+        ic[k].cost = (int64_t)(fv->nseg > 1 ? fv->seglen : fv->n) * 8 + fv->H;
+        ic[k].item = FS_ITEM(v, s, t);
+        k++;
+        if (s < fv->nseg - 1) segitems[ks++] = FS_ITEM(v, s, t);
+      }
     }
   }
   qsort(ic, (size_t)nitems, sizeof(fs_item_cost), cmp_cost_desc);
@@ -140,23 +208,26 @@ static int plan_build(fs_plan *p) {
   free(ic);
   cudaFree(p->items_d);
   p->items_d = NULL;
-  int e = cudaMalloc((void **)&p->items_d, sizeof(int32_t) * (size_t)nitems);
-  if (!e) e = cudaMemcpy(p->items_d, items, sizeof(int32_t) * (size_t)nitems,
+  cudaFree(p->segitems_d);
+  p->segitems_d = NULL;
+  e = cudaMalloc((void **)&p->items_d, sizeof(int64_t) * (size_t)nitems);
+  if (!e) e = cudaMemcpy(p->items_d, items, sizeof(int64_t) * (size_t)nitems,
                          cudaMemcpyHostToDevice);
+  if (!e && ks) e = cudaMalloc((void **)&p->segitems_d, sizeof(int64_t) * (size_t)ks);
+  if (!e && ks)
+    e = cudaMemcpy(p->segitems_d, segitems, sizeof(int64_t) * (size_t)ks, cudaMemcpyHostToDevice);
+  free(segitems);
   free(p->items_h);
   p->items_h = items;
   p->ngroups = 0; /* group lists follow the items */
   if (e) return fs_cuda_fail(ctx, e, "items upload");
   p->nitems = (int32_t)nitems;
+  p->nsegitems = (int32_t)ks;
   e = cudaMemcpy(p->fv_d, p->fv_h, sizeof(FsView) * (size_t)p->nviews, cudaMemcpyHostToDevice);
   if (!e && p->tm_d)
     e = cudaMemcpy(p->tm_d, p->tm_h, sizeof(CUtensorMap) * (size_t)p->nviews,
                    cudaMemcpyHostToDevice);
   if (e) return fs_cuda_fail(ctx, e, "view upload");
-  int32_t occ = 0;
-  e = fsk_render_max_ctas_per_sm(&p->tune, p->hf, p->cf, p->stride_max, &occ);
-  if (e) return fs_cuda_fail(ctx, e, "occupancy query");
-  if (occ < 1) return fs_fail(ctx, FS_ERR_ARG, "render kernel does not fit on an SM");
   int64_t grid = (int64_t)occ * ctx->sm_count;
   if (p->tune.ctas > 0 && p->tune.ctas < grid) grid = p->tune.ctas;
   const int64_t per_cta = fsk_items_per_cta(&p->tune);
@@ -260,12 +331,13 @@ int fs_plan_new(fs_ctx *ctx, fs_plan **out, const fs_map *const *maps, int32_t n
     p->offsets[v] = px;
     px += ((int64_t)vw->width * vw->height + 63) & ~(int64_t)63; /* 256-byte aligned frames */
     if (vw->height > hmax) hmax = vw->height;
+    if (vw->width > p->wmax) p->wmax = vw->width;
   }
   p->ztotal = zoff;
   p->total_px = px;
   p->stride_max = hmax | 1;
   int e = cudaMalloc((void **)&p->fv_d, sizeof(FsView) * (size_t)nviews);
-  if (!e) e = cudaMalloc((void **)&p->head_d, sizeof(int32_t));
+  if (!e) e = cudaMalloc((void **)&p->head_d, 2 * sizeof(int32_t));
   if (!e) e = cudaMalloc((void **)&p->zline, sizeof(float4) * (size_t)zoff);
   if (!e) e = cudaMalloc((void **)&p->zinvz, sizeof(float) * (size_t)zoff);
   if (!e) e = cudaMalloc((void **)&p->frames, sizeof(uint32_t) * (size_t)px);
@@ -310,6 +382,10 @@ int fs_plan_set_cameras(fs_plan *p, const fs_camera *cams, int32_t ncams) {
     nv.zoff = p->fv_h[v].zoff;
     nv.out = p->fv_h[v].out;
     nv.tmap = p->fv_h[v].tmap;
+    /* segments stay as built (from the depth capacity) */
+    nv.nseg = p->fv_h[v].nseg;
+    nv.seglen = p->fv_h[v].seglen;
+    nv.segbuf = p->fv_h[v].segbuf;
     p->fv_h[v] = nv;
     p->views_h[v].cam = cams[v];
   }
@@ -327,7 +403,8 @@ int fs_plan_run(fs_plan *p) {
   cudaSetDevice(ctx->device);
   int e = cudaGraphLaunch(p->exec, ctx->stream);
   if (e) return fs_cuda_fail(ctx, e, "cudaGraphLaunch");
-  ctx->launches += 2;
+  /* depth tables + render, plus the segment-minimum and gap-fill passes */
+  ctx->launches += 2 + (p->nsegitems ? 1 : 0) + (p->segbuf_d ? 1 : 0);
   return FS_OK;
 }
 
@@ -355,7 +432,7 @@ int fs_plan_run_per_view(fs_plan *p) {
     CUtensorMap tm __attribute__((aligned(128)));
     const int have_tm = fs_encode_frame_map(ctx, fv.out, fv.W, fv.H, t.tw, &tm);
     int rc = fs_render_view(ctx, &p->maps[fv.map], &fv, &t, p->zline, p->zinvz,
-                            have_tm ? &tm : NULL);
+                            have_tm ? &tm : NULL, 1);
     if (rc) return rc;
   }
   return FS_OK;
@@ -400,21 +477,21 @@ static int plan_build_groups(fs_plan *p, int32_t groups) {
     p->grp_first[g + 1] = (int32_t)v;
   }
   p->grp_first[groups] = p->nviews;
-  int32_t *sorted = (int32_t *)malloc(sizeof(int32_t) * (size_t)p->nitems);
+  int64_t *sorted = (int64_t *)malloc(sizeof(int64_t) * (size_t)(p->nitems ? p->nitems : 1));
   if (!sorted) return fs_fail(ctx, FS_ERR_NOMEM, "malloc(group items)");
   int32_t k = 0;
   for (int g = 0; g < groups; g++) {
     p->grp_item_off[g] = k;
     for (int32_t i = 0; i < p->nitems; i++) {
-      const int32_t view = p->items_h[i] >> 16;
+      const int32_t view = FS_ITEM_VIEW(p->items_h[i]);
       if (view >= p->grp_first[g] && view < p->grp_first[g + 1]) sorted[k++] = p->items_h[i];
     }
   }
   p->grp_item_off[groups] = k;
   cudaFree(p->grp_items_d);
   p->grp_items_d = NULL;
-  int e = cudaMalloc((void **)&p->grp_items_d, sizeof(int32_t) * (size_t)(k ? k : 1));
-  if (!e) e = cudaMemcpy(p->grp_items_d, sorted, sizeof(int32_t) * (size_t)k, cudaMemcpyHostToDevice);
+  int e = cudaMalloc((void **)&p->grp_items_d, sizeof(int64_t) * (size_t)(k ? k : 1));
+  if (!e) e = cudaMemcpy(p->grp_items_d, sorted, sizeof(int64_t) * (size_t)k, cudaMemcpyHostToDevice);
   free(sorted);
   if (!e && !p->grp_heads_d)
     e = cudaMalloc((void **)&p->grp_heads_d, sizeof(int32_t) * FS_PLAN_MAX_GROUPS);
@@ -444,8 +521,11 @@ int fs_plan_run_download(fs_plan *p, uint32_t *host, int32_t groups) {
   for (int v = 0; v < p->nviews; v++)
     if (p->ncap[v] > max_n) max_n = p->ncap[v];
   int e = cudaMemsetAsync(p->grp_heads_d, 0, sizeof(int32_t) * (size_t)groups, ctx->stream);
+  if (!e) e = cudaMemsetAsync(p->head_d, 0, 2 * sizeof(int32_t), ctx->stream);
   if (!e) e = fsk_ztable(p->fv_d, NULL, p->nviews, max_n, p->zline, p->zinvz, ctx->stream);
+  if (!e) e = plan_segmin(p);
   const int32_t per_cta = fsk_items_per_cta(&p->tune);
+  const FsTune kt = plan_kernel_tune(p);
   for (int g = 0; !e && g < groups; g++) {
     FsLaunch L;
     plan_fill_launch(p, &L);
@@ -454,7 +534,10 @@ int fs_plan_run_download(fs_plan *p, uint32_t *host, int32_t groups) {
     L.head = p->grp_heads_d + g;
     int32_t grid = (L.nitems + per_cta - 1) / per_cta;
     if (grid > p->grid) grid = p->grid;
-    if (L.nitems > 0) e = fsk_render(&L, &p->tune, p->hf, p->cf, grid, ctx->stream);
+    if (L.nitems > 0) e = fsk_render(&L, &kt, p->hf, p->cf, grid, ctx->stream);
+    if (!e && p->segbuf_d)
+      e = fsk_gapfill(p->fv_d + p->grp_first[g], NULL, p->grp_first[g + 1] - p->grp_first[g],
+                      p->wmax, ctx->stream);
     if (!e) e = cudaEventRecord(p->grp_done[g], ctx->stream);
     if (!e) e = cudaStreamWaitEvent(p->copy_stream, p->grp_done[g], 0);
     const int64_t a = p->offsets[p->grp_first[g]];
@@ -463,7 +546,7 @@ int fs_plan_run_download(fs_plan *p, uint32_t *host, int32_t groups) {
       e = cudaMemcpyAsync(host + a, p->frames + a, sizeof(uint32_t) * (size_t)(b - a),
                           cudaMemcpyDeviceToHost, p->copy_stream);
   }
-  ctx->launches += 1 + groups;
+  ctx->launches += 1 + groups + (p->nsegitems ? 1 : 0) + (p->segbuf_d ? groups : 0);
   if (!e) e = cudaStreamSynchronize(p->copy_stream);
   if (e) return fs_cuda_fail(ctx, e, "pipelined render and download");
   return FS_OK;

@@ -27,11 +27,14 @@ struct fs_ctx {
   void *encode; /* cuTensorMapEncodeTiled, NULL when the driver lacks it */
   int32_t use_tma;
   int32_t no_skip; /* 1: ignore the height max pyramid (no chunk skipping) */
+  int32_t no_split; /* 1: never split a column's depth range into segments */
   int32_t sm_count;
   size_t smem_optin;
   float4 *zline; /* single-frame depth table */
   float *zinvz;
   int64_t zcap;
+  int32_t *segbuf; /* single-frame segment minima, final rows, gap flags */
+  int64_t segcap;
   uint32_t *frame_dev; /* device frame for fs_render with host output */
   size_t frame_cap;
   unsigned long long *stats_dev;
@@ -64,9 +67,12 @@ struct fs_plan {
   FsView *fv_d;
   CUtensorMap *tm_h;   /* 128-byte aligned host array */
   CUtensorMap *tm_d;
-  int32_t *items_d;
+  int64_t *items_d;  /* render items (FS_ITEM), launch order */
   int32_t nitems;
-  int32_t *head_d;
+  int64_t *segitems_d; /* segment-minimum items of split views */
+  int32_t nsegitems;
+  int32_t *segbuf_d;   /* segment rows of split views (NULL: none split) */
+  int32_t *head_d;     /* [0] render work counter, [1] segment-minimum counter */
   float4 *zline;
   float *zinvz;
   int64_t ztotal;
@@ -77,19 +83,20 @@ struct fs_plan {
   FsTune tune;
   int32_t grid;
   int32_t stride_max;
+  int32_t wmax; /* widest view */
   int32_t hf, cf;
   cudaGraph_t graph;
   cudaGraphExec_t exec;
   int32_t graph_ok;
   cudaEvent_t ev_render[2]; /* recorded around the render kernel inside the graph */
-  int32_t *items_h;          /* the items in launch order (host copy) */
+  int64_t *items_h;          /* the items in launch order (host copy) */
   /* pipelined render + download (fs_plan_run_download): views split into
    * contiguous groups, each rendered by its own launch while earlier groups'
    * frames are copied to the host on copy_stream */
   int32_t ngroups; /* 0: not built for the current items */
   int32_t grp_first[FS_PLAN_MAX_GROUPS + 1];
   int32_t grp_item_off[FS_PLAN_MAX_GROUPS + 1];
-  int32_t *grp_items_d;
+  int64_t *grp_items_d;
   int32_t *grp_heads_d;
   cudaStream_t copy_stream;
   cudaEvent_t grp_done[FS_PLAN_MAX_GROUPS];
@@ -105,7 +112,10 @@ int fs_ensure_ztable(fs_ctx *ctx, int64_t n);
 int fs_encode_frame_map(fs_ctx *ctx, uint32_t *frame, int32_t W, int32_t H, int32_t tw,
                         CUtensorMap *out);
 int fs_render_view(fs_ctx *ctx, const FsMapDev *map, FsView *v, const FsTune *tune,
-                   float4 *zline, float *zinvz, const CUtensorMap *tmap_pre);
+                   float4 *zline, float *zinvz, const CUtensorMap *tmap_pre, int32_t allow_split);
+int32_t fs_split_target(fs_ctx *ctx, const FsTune *t, int32_t hf, int32_t cf, int32_t stride,
+                        int64_t strips);
+void fs_set_segments(FsView *v, int32_t nseg, int32_t chunk);
 int fs_tune_fits(fs_ctx *ctx, const FsTune *t, int32_t stride_max);
 FsTune fs_tune_for_mode(FsTune t, int32_t view_flags);
 FsTune fs_default_tune(fs_ctx *ctx, int32_t stride_max);

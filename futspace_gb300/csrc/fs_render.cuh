@@ -131,48 +131,113 @@ struct RenderShape {
  * mix(|row - y| / range, previous colour, |y - prev| / range, colour) with
  * range = max(1, prev - row); colour 0 becomes sky, with no gap fill.
  * Compiled for one lane per column and direct painting only.
- * FX = 1: the optional shading / fog epilogue (views with FSV_SHADE/FSV_FOG). */
+ * FX = 1: the optional shading / fog epilogue (views with FSV_SHADE/FSV_FOG).
+ * SEG = 1: direct painting of views split into depth segments (reads the
+ * segment-minimum rows; a separate instantiation so the common kernel keeps
+ * its registers). */
 template <bool B>
 struct BoolTag {
   static constexpr bool value = B;
 };
 
-/* Per-warp state and work of one item: the march over depth chunks, the event
- * ring, colouring and painting. Both kernel layouts call it; `cl` is the lane's
- * column within the item, `c0` the item's first screen column. On return `m`
- * holds the column's final minimum row and `gapcols` (direct painting) has bit
- * c set when column c painted the gap colour. */
+/* What one warp needs to march the columns of an item, held in registers: the
+ * view's fields (the frame stores below may alias the view records as far as
+ * the compiler can tell, so nothing is re-read), the map and the depth table. */
+template <int LC, int U, int HF>
+struct Marcher {
+  static constexpr int CH = LC * U;
+  const FsMapDev &M; /* read in place: no local copy to index */
+  HeightMap hmap;
+  const float4 *zl;
+  const float *zi;
+  float cam_h, horizon, fcol;
+  int H;
+
+  __device__ __forceinline__ Marcher(const FsLaunch &P, const FsView *Vp, int col)
+      : M(P.maps[Vp->map]),
+        hmap{P.maps[Vp->map].q, P.maps[Vp->map].MW, P.maps[Vp->map].MH},
+        zl(P.zline + Vp->zoff),
+        zi(P.zinvz + Vp->zoff),
+        cam_h(Vp->cam_h),
+        horizon(Vp->horizon),
+        fcol((float)col),
+        H(Vp->H) {}
+
+  /* screen row of depth sample k of this lane's column, clamped to [0, H] */
+  template <bool P2>
+  __device__ __forceinline__ int row(int k) const {
+    const float4 L = __ldg(zl + k);
+    const float2 xy = axpy2(fcol, make_float2(L.z, L.w), make_float2(L.x, L.y));
+    const float hh =
+        HF ? height_bilinear<P2>(hmap, xy.x, xy.y) : height_nearest<P2>(hmap, xy.x, xy.y);
+    return min(max(f2i(fa(fm(fs(cam_h, hh), __ldg(zi + k)), horizon)), 0), H);
+  }
+
+  /* Exact skip: rows are monotone in the height and in inv_z, so a row
+   * computed from an upper bound of every height the samples [ka, kb] can read,
+   * at their nearest or farthest depth, bounds every sample's row from below.
+   * If that bound is not above the running minimum m, none of them can lower
+   * it. (Power-of-two maps with a max pyramid only.) */
+  __device__ __forceinline__ bool cannot_lower(int ka, int kb, int m) const {
+    if (m == 0) return true;
+    const float4 La = __ldg(zl + ka), Lb = __ldg(zl + kb);
+    const float iza = __ldg(zi + ka), izb = __ldg(zi + kb);
+    const float2 xa = axpy2(fcol, make_float2(La.z, La.w), make_float2(La.x, La.y));
+    const float2 xb = axpy2(fcol, make_float2(Lb.z, Lb.w), make_float2(Lb.x, Lb.y));
+    const float dh = fs(cam_h, fa((float)segment_max_height(M, xa.x, xa.y, xb.x, xb.y), 1.0f));
+    const int ra = min(max(f2i(fa(fm(dh, iza), horizon)), 0), H);
+    const int rb = min(max(f2i(fa(fm(dh, izb), horizon)), 0), H);
+    return min(ra, rb) >= m;
+  }
+};
+
+/* Depth range [k_begin, k_end) of segment `seg` of a view with n samples. */
+__device__ __forceinline__ void segment_range(const FsView *Vp, int seg, int &k_begin,
+                                              int &k_end) {
+  if (Vp->nseg > 1) {
+    k_begin = seg * Vp->seglen;
+    k_end = min(k_begin + Vp->seglen, Vp->n);
+  } else {
+    k_begin = 0;
+    k_end = Vp->n;
+  }
+}
+
+/* Per-warp work of one item: the march over the depth chunks of [k_begin,
+ * k_end), the event ring, colouring and painting. Both kernel layouts call it;
+ * `cl` is the lane's column within the item, `c0` the item's first screen
+ * column, `m_init` the column's minimum row before k_begin. On return `m`
+ * holds the column's minimum row after k_end and `gapcols` (direct painting)
+ * has bit c set when column c painted the gap colour. */
 template <int TW, int LC, int U, int HF, int CF, int STG, int SM, int FX>
 __device__ __forceinline__ void render_strip(const FsLaunch &P, const FsView *Vp, int c0, int cl,
                                              int lane, unsigned lanemask_lt,
                                              unsigned long long *q, uint32_t *stage,
-                                             const LutChannels &chan, int &m_out,
-                                             uint32_t &gapcols, uint32_t &n_samples,
-                                             uint32_t &n_events) {
+                                             const LutChannels &chan, int k_begin, int k_end,
+                                             int m_init, int &m_out, uint32_t &gapcols,
+                                             uint32_t &n_samples, uint32_t &n_events) {
   using S = RenderShape<TW, LC, U, STG, SM>;
   constexpr int CH = LC * U;
   constexpr int QCAP = S::QCAP;
   const int dl = lane % LC;
-  /* the view's fields live in registers: the frame stores below may alias
-   * the view records as far as the compiler can tell */
-  const float cam_h = Vp->cam_h, horizon = Vp->horizon;
   const int W = Vp->W, H = Vp->H, n = Vp->n;
   const uint32_t sky = Vp->sky, gap = Vp->gap;
   const int vflags = Vp->flags;
+  uint32_t *const out = Vp->out;
+  const int stride = H | 1;
+  const int col = c0 + cl;
+  const bool valid = col < W;
+  const float cam_h = Vp->cam_h, horizon = Vp->horizon;
   const FsMapDev &M = P.maps[Vp->map]; /* read in place: no local copy to index */
   const HeightMap hmap{M.q, M.MW, M.MH};
   const bool p2 = M.pow2 != 0;
   const float4 *zl = P.zline + Vp->zoff;
   const float *zi = P.zinvz + Vp->zoff;
-  uint32_t *const out = Vp->out;
-  const int stride = H | 1;
-  const int col = c0 + cl;
-  const bool valid = col < W;
   const float fcol = (float)col;
 
   /* running minimum row of this column; 0 also marks a column past the
    * frame's right edge, which never has an event */
-  int m = valid ? H : 0;
+  int m = valid ? m_init : 0;
   int qh = 0, qt = 0; /* ring head / tail, warp-uniform */
   uint32_t gapbits = 0;
   /* smoothing: the last event of this lane's column, queued once the sample
@@ -257,7 +322,7 @@ __device__ __forceinline__ void render_strip(const FsLaunch &P, const FsView *Vp
       for (int u = 0; u < U; u++) {
         const int k = k0 + u;
         const int rr = sample_row(p2tag, k);
-        r[u] = k < n ? rr : H;
+        r[u] = k < k_end ? rr : H;
       }
 #pragma unroll
       for (int u = 0; u < U; u++) {
@@ -293,7 +358,7 @@ __device__ __forceinline__ void render_strip(const FsLaunch &P, const FsView *Vp
       for (int u = 0; u < U; u++) {
         const int k = k0 + u * LC + dl;
         const int rr = sample_row(p2tag, k);
-        r[u] = k < n ? rr : H;
+        r[u] = k < k_end ? rr : H;
       }
 #pragma unroll
       for (int u = 0; u < U; u++) {
@@ -320,11 +385,11 @@ __device__ __forceinline__ void render_strip(const FsLaunch &P, const FsView *Vp
 
   /* One loop, one drain site: march a chunk while fewer than 32 events wait,
    * colour and paint 32 at a time, and flush the rest once the march ends. */
-  int k0 = 0;
+  int k0 = k_begin;
   bool marching = true;
   for (;;) {
     if (marching && qt - qh < 32) {
-      if (k0 >= n || __all_sync(FS_FULL_MASK, m == 0)) {
+      if (k0 >= k_end || __all_sync(FS_FULL_MASK, m == 0)) {
         marching = false;
         if constexpr (SM) {
           /* the column's last event: no later sample is an event, so it held
@@ -352,7 +417,7 @@ __device__ __forceinline__ void render_strip(const FsLaunch &P, const FsView *Vp
            * at the chunk's nearest or farthest depth, bounds every sample's
            * row from below. If that bound is not above the running minimum,
            * no sample of the chunk can be an event for this column. */
-          const int ka = kc, kb = min(kc + CH, n) - 1;
+          const int ka = kc, kb = min(kc + CH, k_end) - 1;
           bool lskip = m == 0;
           if (!lskip) {
             const float4 La = __ldg(zl + ka), Lb = __ldg(zl + kb);
@@ -371,7 +436,7 @@ __device__ __forceinline__ void render_strip(const FsLaunch &P, const FsView *Vp
           if (P.stats && m > 0) {
             int c = 0;
 #pragma unroll
-            for (int u = 0; u < U; u++) c += (kc + u * LC + dl < n) ? 1 : 0;
+            for (int u = 0; u < U; u++) c += (kc + u * LC + dl < k_end) ? 1 : 0;
             n_samples += (uint32_t)c;
           }
           if (p2)
@@ -395,7 +460,23 @@ __device__ __forceinline__ void render_strip(const FsLaunch &P, const FsView *Vp
   gapcols = gapbits;
 }
 
-template <int TW, int LC, int U, int HF, int CF, int STG, int SM, int FX>
+/* The view, depth segment and first column of work item `item`. */
+template <int IW>
+__device__ __forceinline__ const FsView *decode_item(const FsLaunch &P, int item, int &seg,
+                                                     int &c0) {
+  if (P.items) {
+    const int64_t it = P.items[item];
+    seg = FS_ITEM_SEG(it);
+    c0 = FS_ITEM_TILE(it) * IW;
+    return P.views + FS_ITEM_VIEW(it);
+  }
+  const int ntiles = (P.view0.W + IW - 1) / IW;
+  seg = item / ntiles;
+  c0 = (item - seg * ntiles) * IW;
+  return &P.view0;
+}
+
+template <int TW, int LC, int U, int HF, int CF, int STG, int SM, int FX, int SEG>
 __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_blocks))
     render_kernel(const __grid_constant__ FsLaunch P) {
   using S = RenderShape<TW, LC, U, STG, SM>;
@@ -426,7 +507,7 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
 
   if constexpr (STG) {
     /* a CTA per (view, tile of TW columns): march into the column stage,
-     * fill, then transpose and store with TMA */
+     * fill, then transpose and store with TMA (whole columns: one segment) */
     __shared__ int s_item;
     const int cl = warp * CPW + lane / LC;
     for (int iter = 0;; iter++) {
@@ -439,20 +520,15 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
         item = iter == 0 ? (int)blockIdx.x : P.nitems;
       }
       if (item >= P.nitems) break;
-      int vi = 0, tile = item;
-      if (P.items) {
-        const int it = P.items[item];
-        vi = it >> 16;
-        tile = it & 0xFFFF;
-      }
-      const FsView *Vp = P.views ? P.views + vi : &P.view0;
-      const int c0 = tile * TW;
+      int seg, c0;
+      const FsView *Vp = decode_item<TW>(P, item, seg, c0);
+      const int W = Vp->W, H = Vp->H, stride = H | 1;
+      const uint32_t sky = Vp->sky, gap = Vp->gap;
       int m;
       uint32_t gapcols;
       render_strip<TW, LC, U, HF, CF, STG, SM, FX>(P, Vp, c0, cl, lane, lanemask_lt, q, stage,
-                                                   chan, m, gapcols, n_samples, n_events);
-      const int W = Vp->W, H = Vp->H, stride = H | 1;
-      const uint32_t sky = Vp->sky, gap = Vp->gap;
+                                                   chan, 0, Vp->n, H, m, gapcols, n_samples,
+                                                   n_events);
       /* gap fill + sky for this warp's columns, then the transposed store */
 #pragma unroll 1
       for (int c = 0; c < CPW; c++) {
@@ -495,7 +571,8 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
     }
     if (tid == 0) bulk_wait_all();
   } else {
-    /* a warp per (view, strip of CPW columns): no barrier between items */
+    /* a warp per (view, depth segment, strip of CPW columns): no barrier
+     * between items */
     const int cl = lane / LC;
     for (int iter = 0;; iter++) {
       int item;
@@ -507,37 +584,55 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
         item = iter == 0 ? (int)blockIdx.x * NW + warp : P.nitems;
       }
       if (item >= P.nitems) break;
-      int vi = 0, strip = item;
-      if (P.items) {
-        const int it = P.items[item];
-        vi = it >> 16;
-        strip = it & 0xFFFF;
+      int seg, c0;
+      const FsView *Vp = decode_item<CPW>(P, item, seg, c0);
+      const int W = Vp->W, H = Vp->H, nseg = Vp->nseg;
+      const int col = c0 + cl;
+      int kb = 0, ke = Vp->n;
+      if constexpr (SEG) segment_range(Vp, seg, kb, ke);
+      /* the column's minimum row before this segment: the minima of the
+       * earlier segments (the segment-minimum pass) */
+      int m0 = H;
+      if constexpr (SEG) {
+        if (seg > 0 && col < W)
+          for (int s = 0; s < seg; s++) m0 = min(m0, __ldg(Vp->segbuf + (size_t)s * W + col));
       }
-      const FsView *Vp = P.views ? P.views + vi : &P.view0;
-      const int c0 = strip * CPW;
       int m;
       uint32_t gapcols;
       render_strip<TW, LC, U, HF, CF, STG, SM, FX>(P, Vp, c0, cl, lane, lanemask_lt, q, stage,
-                                                   chan, m, gapcols, n_samples, n_events);
-      const int W = Vp->W, H = Vp->H;
+                                                   chan, kb, ke, m0, m, gapcols, n_samples,
+                                                   n_events);
       const uint32_t sky = Vp->sky, gap = Vp->gap;
       uint32_t *const out = Vp->out;
-      /* gap fill over the rows of columns that painted the gap colour */
-      while (gapcols) {
-        const int c = __ffs(gapcols) - 1;
-        gapcols &= gapcols - 1;
-        const int mf = __shfl_sync(FS_FULL_MASK, m, c * LC);
-        uint32_t *oc = out + c0 + c;
-        fill_column([oc, W](int y) { return oc + (size_t)y * W; }, mf, H, mf, gap, sky, lane);
+      if (SEG && nseg > 1) {
+        /* gap fill needs the whole column: flag it for the gap-fill pass */
+        while (gapcols) {
+          const int c = __ffs(gapcols) - 1;
+          gapcols &= gapcols - 1;
+          if (lane == 0) Vp->segbuf[(size_t)(nseg + 1) * W + c0 + c] = 1;
+        }
+      } else {
+        /* gap fill over the rows of columns that painted the gap colour */
+        while (gapcols) {
+          const int c = __ffs(gapcols) - 1;
+          gapcols &= gapcols - 1;
+          const int mf = __shfl_sync(FS_FULL_MASK, m, c * LC);
+          uint32_t *oc = out + c0 + c;
+          fill_column([oc, W](int y) { return oc + (size_t)y * W; }, mf, H, mf, gap, sky, lane);
+        }
       }
-      /* sky rows [0, m) of each column: lane (r, c) with c = lane % CPW
-       * writes column c of rows r, r + LC, ... (a row per store for LC = 1) */
-      const int sc = lane % CPW, sr = lane / CPW;
-      const int msc = __shfl_sync(FS_FULL_MASK, m, sc * LC);
-      const int mtop = __reduce_max_sync(FS_FULL_MASK, (unsigned)m);
-      uint32_t *os = out + (size_t)sr * W + c0 + sc;
-      for (int y = sr; y < mtop; y += LC, os += (size_t)LC * W)
-        if (y < msc) __stcs(os, sky);
+      if (!SEG || seg == nseg - 1 || nseg <= 1) {
+        /* the last segment knows the column's final minimum row */
+        if (SEG && nseg > 1 && dl == 0 && col < W) Vp->segbuf[(size_t)nseg * W + col] = m;
+        /* sky rows [0, m) of each column: lane (r, c) with c = lane % CPW
+         * writes column c of rows r, r + LC, ... (a row per store for LC = 1) */
+        const int sc = lane % CPW, sr = lane / CPW;
+        const int msc = __shfl_sync(FS_FULL_MASK, m, sc * LC);
+        const int mtop = __reduce_max_sync(FS_FULL_MASK, (unsigned)m);
+        uint32_t *os = out + (size_t)sr * W + c0 + sc;
+        for (int y = sr; y < mtop; y += LC, os += (size_t)LC * W)
+          if (y < msc) __stcs(os, sky);
+      }
     }
   }
   if (P.stats) {
@@ -551,6 +646,69 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
   }
 }
 
+/* Segment-minimum pass of split views: a warp per (view, segment, strip)
+ * marches the segment's depths from row H and keeps only the minimum row of
+ * each column (no events, no colours); the render pass starts each segment
+ * from the minimum of the segments before it. Segment 0 also clears the
+ * column's gap flag. Items are those of segments 0 .. nseg-2. */
+template <int TW, int LC, int U, int HF>
+__global__ void __launch_bounds__(TW *LC, 1024 / (TW * LC)) segmin_kernel(
+    const __grid_constant__ FsLaunch P) {
+  constexpr int NW = TW * LC / 32;
+  constexpr int CPW = 32 / LC;
+  constexpr int CH = LC * U;
+  static_assert(CH <= FS_ZPAD, "a chunk reads at most FS_ZPAD depth-table entries past n");
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int dl = lane % LC, cl = lane / LC;
+  for (int iter = 0;; iter++) {
+    int item;
+    if (P.head) {
+      int got = 0;
+      if (lane == 0) got = atomicAdd(P.head, 1);
+      item = __shfl_sync(FS_FULL_MASK, got, 0);
+    } else {
+      item = iter == 0 ? (int)blockIdx.x * NW + warp : P.nitems;
+    }
+    if (item >= P.nitems) break;
+    int seg, c0;
+    const FsView *Vp = decode_item<CPW>(P, item, seg, c0);
+    const int W = Vp->W, nseg = Vp->nseg;
+    const int col = c0 + cl;
+    const bool valid = col < W;
+    int kb, ke;
+    segment_range(Vp, seg, kb, ke);
+    const Marcher<LC, U, HF> mc(P, Vp, col);
+    const bool p2 = mc.M.pow2 != 0;
+    int m = valid ? mc.H : 0;
+    auto chunk_min = [&](auto p2tag, int k0) {
+      constexpr bool P2 = decltype(p2tag)::value;
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int k = k0 + u * LC + dl;
+        const int rr = mc.template row<P2>(k);
+        int v = k < ke ? rr : mc.H;
+#pragma unroll
+        for (int off = 1; off < LC; off <<= 1) v = min(v, __shfl_xor_sync(FS_FULL_MASK, v, off, LC));
+        m = min(m, v);
+      }
+    };
+    for (int k0 = kb; k0 < ke; k0 += CH) {
+      if (__all_sync(FS_FULL_MASK, m == 0)) break;
+      if (mc.M.pyr &&
+          __all_sync(FS_FULL_MASK, mc.cannot_lower(k0, min(k0 + CH, ke) - 1, m)))
+        continue;
+      if (p2)
+        chunk_min(BoolTag<true>{}, k0);
+      else
+        chunk_min(BoolTag<false>{}, k0);
+    }
+    if (dl == 0 && valid) {
+      Vp->segbuf[(size_t)seg * W + col] = m;
+      if (seg == 0) Vp->segbuf[(size_t)(nseg + 1) * W + col] = 0;
+    }
+  }
+}
+
 }  // namespace fsd
 
 /* Kernel modes beyond the plain render, each compiled for a few configurations
@@ -558,6 +716,10 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
  * is its own instantiation because its code, present but unused, makes the
  * plain kernel measurably slower. */
 #define FS_TUNE_LIST_MODES(X) \
+  X(8, 32, 2, 1, 0, 1)        \
+  X(16, 16, 2, 1, 0, 1)       \
+  X(32, 8, 4, 0, 0, 1)        \
+  X(64, 2, 4, 0, 0, 1)        \
   X(64, 1, 4, 0, 0, 1)        \
   X(128, 1, 4, 0, 0, 1)       \
   X(128, 1, 8, 0, 0, 1)       \

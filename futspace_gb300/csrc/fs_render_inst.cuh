@@ -14,12 +14,16 @@ extern "C" int FS_RENDER_ENTRY(int op, const FsLaunch *L, const FsTune *t, int g
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return (int)e;
   if (dev < 0 || dev >= 64) return (int)cudaErrorInvalidDevice;
-#define FS_CASE(TW_, LC_, U_, STG_) FS_CASE_M(TW_, LC_, U_, STG_, 0, 0)
-#define FS_CASE_M(TW_, LC_, U_, STG_, SM_, FX_)                                              \
+#define FS_CASE(TW_, LC_, U_, STG_) \
+  FS_CASE_S(TW_, LC_, U_, STG_, 0, 0, 0) FS_CASE_S(TW_, LC_, U_, STG_, 0, 0, 1)
+#define FS_CASE_M(TW_, LC_, U_, STG_, SM_, FX_) FS_CASE_S(TW_, LC_, U_, STG_, SM_, FX_, 0)
+/* SEG: kernels that read depth segments, for direct painting only (a staged
+ * configuration maps to its one kernel) */
+#define FS_CASE_S(TW_, LC_, U_, STG_, SM_, FX_, SEG_)                                        \
   if (t->tw == TW_ && t->lc == LC_ && t->u == U_ && t->stage == STG_ && t->smooth == SM_ &&  \
-      t->fx == FX_) {                                                                       \
+      t->fx == FX_ && (t->seg != 0) == (SEG_ != 0)) {                                       \
     static int smem_set[64];                                                               \
-    auto kern = fsd::render_kernel<TW_, LC_, U_, FS_HF, FS_CF, STG_, SM_, FX_>;             \
+    auto kern = fsd::render_kernel<TW_, LC_, U_, FS_HF, FS_CF, STG_, SM_, FX_, (SEG_ && !STG_)>; \
     if (smem_set[dev] < (int)smem) {                                                       \
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
       if (e != cudaSuccess) return (int)e;                                                 \
@@ -34,5 +38,21 @@ extern "C" int FS_RENDER_ENTRY(int op, const FsLaunch *L, const FsTune *t, int g
   FS_TUNE_LIST_MODES(FS_CASE_M)
 #undef FS_CASE
 #undef FS_CASE_M
+#undef FS_CASE_S
   return (int)cudaErrorInvalidValue;
 }
+
+#if FS_CF == 0
+/* The segment-minimum pass (no colours: compiled once per height filter) for
+ * every direct-paint configuration. */
+extern "C" int FS_SEGMIN_ENTRY(const FsLaunch *L, const FsTune *t, int grid, cudaStream_t st) {
+#define FS_SEG_CASE(TW_, LC_, U_, STG_)                                   \
+  if (STG_ == 0 && t->tw == TW_ && t->lc == LC_ && t->u == U_ && !t->stage) { \
+    fsd::segmin_kernel<TW_, LC_, U_, FS_HF><<<grid, TW_ * LC_, 0, st>>>(*L); \
+    return (int)cudaGetLastError();                                       \
+  }
+  FS_TUNE_LIST(FS_SEG_CASE)
+#undef FS_SEG_CASE
+  return (int)cudaErrorInvalidValue;
+}
+#endif

@@ -107,7 +107,8 @@ typedef struct {
   int32_t busy;
   int32_t nreq;
   int32_t *req;    /* request indices of the launch */
-  uint8_t *pinned; /* [FsView x max_batch][int32 ids x max_batch][int32 items x max_items] */
+  uint8_t *pinned; /* [FsView x max_batch][int32 ids x max_batch, padded to 8 bytes]
+                      [int64 items x max_items] */
   uint8_t *dev;    /* same layout on the device */
   int32_t *head_d;
 } fs_slot;
@@ -161,9 +162,13 @@ void fs_server_free(fs_server *s) {
   free(s);
 }
 
+/* Byte offset of the work items in a slot buffer (8-byte aligned). */
+static size_t items_offset(const fs_server *s) {
+  return (sizeof(FsView) * (size_t)s->cfg.max_batch + 4 * (size_t)s->cfg.max_batch + 7) & ~(size_t)7;
+}
+
 static size_t slot_bytes(const fs_server *s) {
-  return sizeof(FsView) * (size_t)s->cfg.max_batch + 4 * (size_t)s->cfg.max_batch +
-         4 * (size_t)s->max_items;
+  return items_offset(s) + 8 * (size_t)s->max_items;
 }
 
 int fs_server_new(fs_ctx *ctx, fs_server **out, const fs_map *const *maps, int32_t nmaps,
@@ -262,13 +267,13 @@ int fs_server_new(fs_ctx *ctx, fs_server **out, const fs_map *const *maps, int32
 
 typedef struct {
   int64_t cost;
-  int32_t item;
+  int64_t item;
 } srv_item;
 
 static int cmp_item(const void *a, const void *b) {
   const srv_item *x = (const srv_item *)a, *y = (const srv_item *)b;
   if (x->cost != y->cost) return x->cost > y->cost ? -1 : 1;
-  return x->item - y->item;
+  return (x->item > y->item) - (x->item < y->item);
 }
 
 typedef struct {
@@ -293,7 +298,7 @@ static int launch_batch(fs_server *s, fs_slot *sl, fs_request *reqs, fs_fifo *re
   const int32_t mb = s->cfg.max_batch;
   FsView *packed = (FsView *)sl->pinned;
   int32_t *ids = (int32_t *)(sl->pinned + sizeof(FsView) * (size_t)mb);
-  int32_t *items = ids + mb;
+  int64_t *items = (int64_t *)(sl->pinned + items_offset(s));
   int32_t nb = 0, ni = 0;
   sl->nreq = 0;
   while (ready->head < ready->tail && nb < mb) {
@@ -323,7 +328,7 @@ static int launch_batch(fs_server *s, fs_slot *sl, fs_request *reqs, fs_fifo *re
     ids[nb] = r->session;
     for (int32_t t = 0; t < tiles; t++) {
       scratch[ni].cost = (int64_t)v.n * 8 + v.H;
-      scratch[ni].item = (r->session << 16) | t;
+      scratch[ni].item = FS_ITEM(r->session, 0, t);
       ni++;
     }
     sl->req[nb] = ri;
@@ -335,11 +340,11 @@ static int launch_batch(fs_server *s, fs_slot *sl, fs_request *reqs, fs_fifo *re
   qsort(scratch, (size_t)ni, sizeof(srv_item), cmp_item);
   for (int32_t i = 0; i < ni; i++) items[i] = scratch[i].item;
   sl->nreq = nb;
-  const size_t used = sizeof(FsView) * (size_t)mb + 4 * (size_t)mb + 4 * (size_t)ni;
+  const size_t used = items_offset(s) + 8 * (size_t)ni;
   int e = cudaMemcpyAsync(sl->dev, sl->pinned, used, cudaMemcpyHostToDevice, sl->st);
   const FsView *packed_d = (const FsView *)sl->dev;
   const int32_t *ids_d = (const int32_t *)(sl->dev + sizeof(FsView) * (size_t)mb);
-  const int32_t *items_d = ids_d + mb;
+  const int64_t *items_d = (const int64_t *)(sl->dev + items_offset(s));
   int32_t max_n = 0;
   for (int32_t i = 0; i < nb; i++)
     if (packed[i].n > max_n) max_n = packed[i].n;

@@ -122,7 +122,8 @@ typedef struct {
 static int frame_once(void *arg) {
   frame_job *j = (frame_job *)arg;
   FsView v = j->view;
-  return fs_render_view(j->ctx, &j->map->dev, &v, &j->tune, j->ctx->zline, j->ctx->zinvz, NULL);
+  return fs_render_view(j->ctx, &j->map->dev, &v, &j->tune, j->ctx->zline, j->ctx->zinvz, NULL,
+                        1);
 }
 
 /* Times every fitting configuration on one frame and caches the fastest for

@@ -120,9 +120,12 @@ int64_t fs_ctx_kernel_launches(fs_ctx *ctx);
  * render; NULL or tile width 0 restores the tuning-cache / default choice. */
 int fs_ctx_force_tune(fs_ctx *ctx, const int32_t tune5[5]);
 /* Context options: "skip" (1, default: skip depth chunks that a max-pyramid
- * bound proves cannot change the frame; 0: march every depth sample) and "tma"
+ * bound proves cannot change the frame; 0: march every depth sample), "tma"
  * (1, default when the driver provides tensor maps: TMA row stores from the
- * staged kernels; 0: plain stores). Plans capture the options at creation or
+ * staged kernels; 0: plain stores) and "split" (1, default: when a launch has
+ * too few column strips to occupy the GPU, split each column's depth range
+ * into segments marched by separate warps, after a pass that finds each
+ * segment's minimum row; 0: never). Plans capture the options at creation or
  * retuning. Pixels are identical either way. */
 int fs_ctx_set_option(fs_ctx *ctx, const char *name, int64_t value);
 

@@ -269,3 +269,53 @@ def test_smoothing_branch(fs, orc, gpu_ctx, maps256, hf, cf):
     with pytest.raises(fs.FsError):
         gpu_ctx.render(fmap, views[0][0], 64, 48,
                        params=fs.default_params(smoothing=1, gap_rule=1))
+
+
+@pytest.mark.parametrize("hf,cf", [(1, 1), (0, 1)])
+def test_depth_segments_exact(fs, orc, gpu_ctx, maps1024, hf, cf):
+    """Columns split into depth segments (segment-minimum pass, render pass from
+    the prefix minimum, gap-fill pass) give the same frames as unsplit columns,
+    for single frames and plans, with zero texels forcing the gap fill."""
+    hm, cm = maps1024
+    cm = cm.copy()
+    cm[::5, ::3] = 0          # gap colour (gap rule 0) in the map
+    fmap = fs.Map(gpu_ctx, hm, cm)
+    p = fs.default_params(height_filter=hf, color_filter=cf)
+    views = _mixed_views(fs, hm, 131 + hf + 2 * cf, 6)
+    refs = [_oracle(orc, c, p, hm, cm, w, h) for c, w, h in views]
+    direct = [t for t in fs.tune_table() if t[3] == 0]
+    for tune in direct[::3]:
+        gpu_ctx.force_tune(tune)
+        splits = 0
+        for (c, w, h), r in zip(views, refs):
+            l0 = gpu_ctx.launches
+            got = gpu_ctx.render(fmap, c, w, h, params=p)
+            assert count_diff(got, r) == 0, (tune, w, h)
+            splits += gpu_ctx.launches - l0 > 2
+            gpu_ctx.set_option("split", 0)
+            l0 = gpu_ctx.launches
+            assert count_diff(gpu_ctx.render(fmap, c, w, h, params=p), r) == 0
+            assert gpu_ctx.launches - l0 == 2
+            gpu_ctx.set_option("split", 1)
+        assert splits > 0, tune  # frames this small have too few strips: they split
+    gpu_ctx.force_tune(None)
+    # a plan of few views splits too; shorter draw distances later leave
+    # trailing segments empty
+    plan = fs.Plan(gpu_ctx, [fmap], views, params=p)
+    for tune in direct[::4]:
+        plan.set_tune(*tune)
+        plan.run()
+        assert all(count_diff(f, r) == 0 for f, r in zip(plan.frames(), refs)), tune
+    cams = []
+    for c, w, h in views:
+        d = fs.Camera(*c.as_tuple())
+        d.distance = c.distance * 0.5
+        cams.append(d)
+    plan.set_cameras(cams)
+    plan.run()
+    for i, ((c, w, h), f) in enumerate(zip(views, plan.frames())):
+        assert count_diff(f, _oracle(orc, cams[i], p, hm, cm, w, h)) == 0
+    buf = fs.PinnedBuffer(plan.total_pixels)
+    flat = plan.run_download(buf.array, groups=3)
+    for i, ((c, w, h), f) in enumerate(zip(views, plan.frames(flat))):
+        assert count_diff(f, _oracle(orc, cams[i], p, hm, cm, w, h)) == 0
