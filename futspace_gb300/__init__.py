@@ -111,10 +111,6 @@ def _release_all():
 atexit.register(_release_all)
 
 
-def _finalizing() -> bool:
-    return sys.is_finalizing()
-
-
 def _sig(lib, name, res, args):
     f = getattr(lib, name)
     f.restype = res
@@ -391,8 +387,10 @@ class Context:
     def __exit__(self, *a):
         self.close()
 
-    def __del__(self):
-        if _finalizing():
+    def __del__(self, _fin=sys.is_finalizing):
+        # the default binds the check at class creation: module globals may
+        # already be gone when a late collection runs this
+        if _fin():
             return
         try:
             self.close()
@@ -470,8 +468,10 @@ class Map:
             lib().fs_map_free(self.ctx.handle, self._h)
             self._h = C.c_void_p()
 
-    def __del__(self):
-        if _finalizing():
+    def __del__(self, _fin=sys.is_finalizing):
+        # the default binds the check at class creation: module globals may
+        # already be gone when a late collection runs this
+        if _fin():
             return
         try:
             self.close()
@@ -575,8 +575,10 @@ class Plan:
             lib().fs_plan_free(self._h)
             self._h = C.c_void_p()
 
-    def __del__(self):
-        if _finalizing():
+    def __del__(self, _fin=sys.is_finalizing):
+        # the default binds the check at class creation: module globals may
+        # already be gone when a late collection runs this
+        if _fin():
             return
         try:
             self.close()
@@ -606,8 +608,10 @@ class PinnedBuffer:
             lib().fs_host_free(self._p)
             self._p = None
 
-    def __del__(self):
-        if _finalizing():
+    def __del__(self, _fin=sys.is_finalizing):
+        # the default binds the check at class creation: module globals may
+        # already be gone when a late collection runs this
+        if _fin():
             return
         try:
             self.close()
@@ -644,8 +648,10 @@ class Server:
             lib().fs_server_free(self._h)
             self._h = C.c_void_p()
 
-    def __del__(self):
-        if _finalizing():
+    def __del__(self, _fin=sys.is_finalizing):
+        # the default binds the check at class creation: module globals may
+        # already be gone when a late collection runs this
+        if _fin():
             return
         try:
             self.close()

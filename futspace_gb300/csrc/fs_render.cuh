@@ -48,6 +48,7 @@ template <int U>
 struct QueueCap {
   static constexpr int raw = 31 + 32 * U;
   static constexpr int value = raw <= 64 ? 64 : (raw <= 128 ? 128 : (raw <= 256 ? 256 : 512));
+  static_assert(raw <= value, "ring too small for 31 waiting events plus one chunk");
 };
 
 constexpr int kBoxRows = 32;
