@@ -304,8 +304,14 @@ __device__ __forceinline__ void render_strip(const FsLaunch &P, const FsView *Vp
         uint32_t *sc = stage + ecl * stride;
         for (int yy = er; yy < ep; yy++) sc[yy] = colour;
       } else {
+        /* most intervals are a few rows: the first four stores are predicated
+         * straight-line code, the rest a loop */
         uint32_t *o = out + (size_t)er * W + c0 + ecl;
-        for (int yy = er; yy < ep; yy++, o += W) __stcs(o, colour);
+        const int len = ep - er;
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+          if (j < len) __stcs(o + (size_t)j * W, colour);
+        for (int j = 4; j < len; j++) __stcs(o + (size_t)j * W, colour);
         if (colour == gap) gb = 1u << ecl;
       }
     }
