@@ -143,17 +143,17 @@ __device__ __forceinline__ float height_nearest(const FsMapDev &M, float x, floa
   return byte_f(__ldg(M.q + (size_t)iy * (size_t)M.MW + ix), 0x7540);
 }
 
-/* Upper bound of every height the samplers can read for samples on the segment
- * between (xa, ya) and (xb, yb): the max pyramid over the texel box
- * [floor(min x) - 1, floor(max x) + 2] x (same in y), which holds every
- * bilinear corner of every sample on the segment with a margin for rounding,
- * at the level where the box spans at most 2 x 2 cells (4 lookups). */
-__device__ __forceinline__ int segment_max_height(const FsMapDev &M, float xa, float ya, float xb,
-                                                  float yb) {
+/* Upper bound of every height the samplers can read for samples whose
+ * coordinates lie in [x0, x1] x [y0, y1]: the max pyramid over the texel box
+ * [floor(x0) - 1, floor(x1) + 2] x (same in y), which holds every bilinear
+ * corner of every such sample with a margin for rounding, at the level where
+ * the box spans at most 2 x 2 cells (4 lookups). */
+__device__ __forceinline__ int box_max_height(const FsMapDev &M, float x0, float x1, float y0,
+                                              float y1) {
   const float lim = 1.0e9f; /* also rejects NaN */
-  if (!(fabsf(xa) < lim && fabsf(xb) < lim && fabsf(ya) < lim && fabsf(yb) < lim)) return 255;
-  const int ix0 = __float2int_rd(fminf(xa, xb)) - 1, ix1 = __float2int_rd(fmaxf(xa, xb)) + 2;
-  const int iy0 = __float2int_rd(fminf(ya, yb)) - 1, iy1 = __float2int_rd(fmaxf(ya, yb)) + 2;
+  if (!(fabsf(x0) < lim && fabsf(x1) < lim && fabsf(y0) < lim && fabsf(y1) < lim)) return 255;
+  const int ix0 = __float2int_rd(x0) - 1, ix1 = __float2int_rd(x1) + 2;
+  const int iy0 = __float2int_rd(y0) - 1, iy1 = __float2int_rd(y1) + 2;
   const int span = max(ix1 - ix0, iy1 - iy0) + 1;
   const int L = 32 - __clz(span - 1); /* ceil(log2(span)): cells of 2^L texels */
   if (L > M.pyr_levels) return 255;
@@ -164,6 +164,12 @@ __device__ __forceinline__ int segment_max_height(const FsMapDev &M, float xa, f
   const int a = max(__ldg(P + cy0 * cw + cx0), __ldg(P + cy0 * cw + cx1));
   const int b = max(__ldg(P + cy1 * cw + cx0), __ldg(P + cy1 * cw + cx1));
   return max(a, b);
+}
+
+/* The same over the segment between (xa, ya) and (xb, yb). */
+__device__ __forceinline__ int segment_max_height(const FsMapDev &M, float xa, float ya, float xb,
+                                                  float yb) {
+  return box_max_height(M, fminf(xa, xb), fmaxf(xa, xb), fminf(ya, yb), fmaxf(ya, yb));
 }
 
 /* ---- matte 0.1.2 argb colour arithmetic (to_rgba / from_rgba / mix) ----------

@@ -173,23 +173,6 @@ struct Marcher {
         HF ? height_bilinear<P2>(hmap, xy.x, xy.y) : height_nearest<P2>(hmap, xy.x, xy.y);
     return min(max(f2i(fa(fm(fs(cam_h, hh), __ldg(zi + k)), horizon)), 0), H);
   }
-
-  /* Exact skip: rows are monotone in the height and in inv_z, so a row
-   * computed from an upper bound of every height the samples [ka, kb] can read,
-   * at their nearest or farthest depth, bounds every sample's row from below.
-   * If that bound is not above the running minimum m, none of them can lower
-   * it. (Power-of-two maps with a max pyramid only.) */
-  __device__ __forceinline__ bool cannot_lower(int ka, int kb, int m) const {
-    if (m == 0) return true;
-    const float4 La = __ldg(zl + ka), Lb = __ldg(zl + kb);
-    const float iza = __ldg(zi + ka), izb = __ldg(zi + kb);
-    const float2 xa = axpy2(fcol, make_float2(La.z, La.w), make_float2(La.x, La.y));
-    const float2 xb = axpy2(fcol, make_float2(Lb.z, Lb.w), make_float2(Lb.x, Lb.y));
-    const float dh = fs(cam_h, fa((float)segment_max_height(M, xa.x, xa.y, xb.x, xb.y), 1.0f));
-    const int ra = min(max(f2i(fa(fm(dh, iza), horizon)), 0), H);
-    const int rb = min(max(f2i(fa(fm(dh, izb), horizon)), 0), H);
-    return min(ra, rb) >= m;
-  }
 };
 
 /* Depth range [k_begin, k_end) of segment `seg` of a view with n samples. */
@@ -203,6 +186,57 @@ __device__ __forceinline__ void segment_range(const FsView *Vp, int seg, int &k_
     k_end = Vp->n;
   }
 }
+
+/* Exact skip bound: rows are monotone in the height and in inv_z, so a row
+ * computed from an upper bound of every height the samples of columns
+ * [cf, cl] at depths [ka, kb] can read, at the nearest or farthest of those
+ * depths, bounds every such sample's row from below. Sample coordinates are
+ * bilinear in (column, depth along the view line), so the four corner samples
+ * bound the box. A chunk whose bound is not above any of the strip's running
+ * minima holds no event. (Power-of-two maps with a max pyramid only.) */
+__device__ __forceinline__ int chunk_row_bound(const FsMapDev &M, const float4 *zl,
+                                               const float *zi, float cam_h, float horizon,
+                                               int H, float cf, float cl, int ka, int kb) {
+  const float4 La = __ldg(zl + ka), Lb = __ldg(zl + kb);
+  const float iza = __ldg(zi + ka), izb = __ldg(zi + kb);
+  const float2 a0 = axpy2(cf, make_float2(La.z, La.w), make_float2(La.x, La.y));
+  const float2 a1 = axpy2(cl, make_float2(La.z, La.w), make_float2(La.x, La.y));
+  const float2 b0 = axpy2(cf, make_float2(Lb.z, Lb.w), make_float2(Lb.x, Lb.y));
+  const float2 b1 = axpy2(cl, make_float2(Lb.z, Lb.w), make_float2(Lb.x, Lb.y));
+  const float x0 = fminf(fminf(a0.x, a1.x), fminf(b0.x, b1.x));
+  const float x1 = fmaxf(fmaxf(a0.x, a1.x), fmaxf(b0.x, b1.x));
+  const float y0 = fminf(fminf(a0.y, a1.y), fminf(b0.y, b1.y));
+  const float y1 = fmaxf(fmaxf(a0.y, a1.y), fmaxf(b0.y, b1.y));
+  const float dh = fs(cam_h, fa((float)box_max_height(M, x0, x1, y0, y1), 1.0f));
+  const int ra = min(max(f2i(fa(fm(dh, iza), horizon)), 0), H);
+  const int rb = min(max(f2i(fa(fm(dh, izb), horizon)), 0), H);
+  return min(ra, rb);
+}
+
+/* Skip bounds of 32 chunks at a time: lane j holds the bound of the chunk
+ * that starts at depth base + j * CH, so one pass of the bound arithmetic
+ * serves 32 chunks; each chunk then costs a shuffle and a max-reduction.
+ * [wfirst, wlast] are the warp's screen columns. */
+template <int CH>
+struct ChunkBounds {
+  int bound = 0;
+  int base = -(1 << 30); /* first depth of lane 0's chunk */
+  /* true when the chunk [kc, kc + CH) of a march ending at k_end can be skipped */
+  __device__ __forceinline__ bool skip(const FsMapDev &M, const float4 *zl, const float *zi,
+                                       float cam_h, float horizon, int H, int wfirst, int wlast,
+                                       int kc, int k_end, int m, int lane) {
+    if (kc >= base + 32 * CH) {
+      base = kc;
+      const int ka = kc + lane * CH;
+      bound = H + 1; /* past the end: never consulted */
+      if (ka < k_end)
+        bound = chunk_row_bound(M, zl, zi, cam_h, horizon, H, (float)wfirst, (float)wlast, ka,
+                                min(ka + CH, k_end) - 1);
+    }
+    const int b = __shfl_sync(FS_FULL_MASK, bound, (kc - base) / CH);
+    return b >= (int)__reduce_max_sync(FS_FULL_MASK, (unsigned)m);
+  }
+};
 
 /* Per-warp work of one item: the march over the depth chunks of [k_begin,
  * k_end), the event ring, colouring and painting. Both kernel layouts call it;
@@ -394,6 +428,7 @@ __device__ __forceinline__ void render_strip(const FsLaunch &P, const FsView *Vp
    * colour and paint 32 at a time, and flush the rest once the march ends. */
   int k0 = k_begin;
   bool marching = true;
+  ChunkBounds<CH> cb;
   for (;;) {
     if (marching && qt - qh < 32) {
       if (k0 >= k_end || __all_sync(FS_FULL_MASK, m == 0)) {
@@ -417,28 +452,11 @@ __device__ __forceinline__ void render_strip(const FsLaunch &P, const FsView *Vp
       } else {
         const int kc = k0;
         k0 += CH;
-        bool skip = false;
-        if (M.pyr) {
-          /* Exact skip: rows are monotone in the height and in inv_z, so a
-           * row computed from an upper bound of every height in the chunk,
-           * at the chunk's nearest or farthest depth, bounds every sample's
-           * row from below. If that bound is not above the running minimum,
-           * no sample of the chunk can be an event for this column. */
-          const int ka = kc, kb = min(kc + CH, k_end) - 1;
-          bool lskip = m == 0;
-          if (!lskip) {
-            const float4 La = __ldg(zl + ka), Lb = __ldg(zl + kb);
-            const float iza = __ldg(zi + ka), izb = __ldg(zi + kb);
-            const float2 xa = axpy2(fcol, make_float2(La.z, La.w), make_float2(La.x, La.y));
-            const float2 xb = axpy2(fcol, make_float2(Lb.z, Lb.w), make_float2(Lb.x, Lb.y));
-            const float dh =
-                fs(cam_h, fa((float)segment_max_height(M, xa.x, xa.y, xb.x, xb.y), 1.0f));
-            const int ra = min(max(f2i(fa(fm(dh, iza), horizon)), 0), H);
-            const int rb = min(max(f2i(fa(fm(dh, izb), horizon)), 0), H);
-            lskip = min(ra, rb) >= m;
-          }
-          skip = __all_sync(FS_FULL_MASK, lskip);
-        }
+        /* the warp's columns: [c0 + cl - lane / LC, + CPW) within the frame */
+        const bool skip =
+            M.pyr && cb.skip(M, zl, zi, cam_h, horizon, H, c0 + cl - lane / LC,
+                             max(c0 + cl - lane / LC, min(c0 + cl - lane / LC + S::CPW, W) - 1), kc,
+                             k_end, m, lane);
         if (!skip) {
           if (P.stats && m > 0) {
             int c = 0;
@@ -699,10 +717,12 @@ __global__ void __launch_bounds__(TW *LC, 1024 / (TW * LC)) segmin_kernel(
         m = min(m, v);
       }
     };
+    ChunkBounds<CH> cb;
+    const int wlast = max(c0, min(c0 + CPW, W) - 1);
     for (int k0 = kb; k0 < ke; k0 += CH) {
       if (__all_sync(FS_FULL_MASK, m == 0)) break;
       if (mc.M.pyr &&
-          __all_sync(FS_FULL_MASK, mc.cannot_lower(k0, min(k0 + CH, ke) - 1, m)))
+          cb.skip(mc.M, mc.zl, mc.zi, mc.cam_h, mc.horizon, mc.H, c0, wlast, k0, ke, m, lane))
         continue;
       if (p2)
         chunk_min(BoolTag<true>{}, k0);
