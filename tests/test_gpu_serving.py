@@ -107,3 +107,33 @@ def test_budget_admission(fs, gpu_ctx, maps256):
         srv.close()
         for b in bufs:
             b.close()
+
+
+@pytest.mark.parametrize("mode", ["smoothing", "effects"])
+def test_serving_modes(fs, orc, gpu_ctx, maps256, mode):
+    """A server built with the smoothing branch or the shading/fog epilogue
+    renders every request as the oracle does in that mode, alone or mixed."""
+    hm, cm = maps256
+    fmap = fs.Map(gpu_ctx, hm, cm)
+    if mode == "smoothing":
+        p = fs.default_params(smoothing=1)
+    else:
+        p = fs.default_params(effects=3, shade=0.5, fog_start=40.0, fog_end=350.0,
+                              fog_color=0xFFB0B8C8)
+    specs = [(s, 0, w, h, cam) for s, (w, h) in enumerate(SIZES)
+             for cam in fs.gen_walk(40 + s, hm, 2, step=2.0, yaw=0.05, above=(20, 120),
+                                    distance=400.0, screen_h=h)]
+    bufs = [fs.PinnedBuffer((h, w)) for (_, _, w, h, _) in specs]
+    srv = fs.Server(gpu_ctx, [fmap], budget_bytes=8 << 20, nsessions=len(SIZES), max_batch=8,
+                    slots=2, max_distance=400.0, params=p)
+    try:
+        reqs = _fill(fs, specs, bufs)
+        st = srv.run(reqs)
+        assert st["errors"] == 0
+        for i, (s, m, w, h, cam) in enumerate(specs):
+            ref = orc.render(cam, orc.params_from(p), hm, cm, w, h, threads=0)
+            assert count_diff(bufs[i].array, ref) == 0, (mode, i)
+    finally:
+        srv.close()
+        for b in bufs:
+            b.close()
