@@ -34,6 +34,8 @@ sys.path.insert(0, str(ROOT))
 
 RESOLUTIONS = [(320, 240), (640, 480), (1280, 720), (1920, 1080), (2560, 1440)]
 MAP_SEED_H, MAP_SEED_C, VIEW_SEED = 7, 8, 20240601
+# the metric both arms report (Gpix/s = total frame pixels / time)
+METRIC = "Gpix/s (bit-exact voxel-space frames), batched multi-view"
 
 
 def batch_views(fs, hm, nviews: int, seed: int):
@@ -215,7 +217,7 @@ def run_reference(args, rank: int, world: int):
             dts += dt
     value = pxs / dts / 1e9
     line = {
-        "impl": "reference", "metric": "Gpix/s (bit-exact voxel-space frames)", "value": value,
+        "impl": "reference", "metric": METRIC, "value": value,
         "unit": "Gpix/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * dts / max(1, args.steps), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
@@ -476,7 +478,7 @@ def main():
     if rank == 0:
         full_s = sum(fs.num_depths(v[0].distance) * v[1] for v in views)
         line = {
-            "metric": "Gpix/s (bit-exact voxel-space frames), batched multi-view",
+            "metric": METRIC,
             "value": value, "unit": "Gpix/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
