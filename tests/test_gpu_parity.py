@@ -319,3 +319,25 @@ def test_depth_segments_exact(fs, orc, gpu_ctx, maps1024, hf, cf):
     flat = plan.run_download(buf.array, groups=3)
     for i, ((c, w, h), f) in enumerate(zip(views, plan.frames(flat))):
         assert count_diff(f, _oracle(orc, cams[i], p, hm, cm, w, h)) == 0
+
+
+def test_degenerate_screen_sizes(fs, orc, gpu_ctx, maps256):
+    """One-pixel and one-row/one-column screens, tall thin and short wide ones,
+    with the default (possibly split) configuration and every direct-paint
+    configuration."""
+    hm, cm = maps256
+    fmap = fs.Map(gpu_ctx, hm, cm)
+    p = fs.default_params()
+    cam = fs.gen_cameras(151, hm, 1, above=(30, 30), distance=(600, 600), screen_h=64)[0]
+    sizes = [(1, 1), (1, 9), (9, 1), (3, 300), (300, 3), (33, 17), (65, 2)]
+    for tune in [None] + [t for t in fs.tune_table() if t[3] == 0][::4]:
+        gpu_ctx.force_tune(tune)
+        for w, h in sizes:
+            got = gpu_ctx.render(fmap, cam, w, h, params=p)
+            assert got.shape == (h, w)
+            assert count_diff(got, _oracle(orc, cam, p, hm, cm, w, h)) == 0, (tune, w, h)
+    gpu_ctx.force_tune(None)
+    plan = fs.Plan(gpu_ctx, [fmap], [(cam, w, h) for w, h in sizes])
+    plan.run()
+    for (w, h), f in zip(sizes, plan.frames()):
+        assert count_diff(f, _oracle(orc, cam, p, hm, cm, w, h)) == 0, (w, h)
