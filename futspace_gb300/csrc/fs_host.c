@@ -469,14 +469,16 @@ const uint32_t *fs_map_colors_dev(const fs_map *map) { return map ? map->dev.c :
 /* ---- tuning ---------------------------------------------------------------- */
 
 /* Compiled configurations {tw, lc, u, stage, ctas}, in the order a single
- * frame tries them when the tuning cache has no entry (first that fits wins). */
+ * frame tries them when the tuning cache has no entry (first that fits wins).
+ * Stage 0 paints directly, 1 through the shared-memory stage, 2 is the
+ * cooperative tile (lc = threads per column, u = depths per thread per block). */
 static const FsTune k_tune_order[] = {
-    {4, 32, 2, 1, 0},  {8, 32, 2, 1, 0},  {8, 32, 1, 1, 0}, {16, 32, 2, 1, 0},
+    {8, 64, 8, 2, 0},  {4, 32, 2, 1, 0},  {8, 32, 2, 1, 0},  {8, 32, 1, 1, 0}, {16, 32, 2, 1, 0},
     {32, 32, 1, 1, 0}, {16, 16, 2, 1, 0}, {32, 16, 2, 1, 0}, {16, 8, 4, 1, 0},
     {32, 8, 4, 1, 0},  {8, 32, 2, 0, 0},  {16, 16, 2, 0, 0}, {32, 8, 2, 0, 0},
     {32, 8, 4, 0, 0},  {32, 4, 4, 0, 0},  {64, 4, 4, 0, 0},  {32, 4, 8, 0, 0},
     {64, 2, 4, 0, 0},  {64, 1, 4, 0, 0},  {128, 1, 4, 0, 0}, {64, 1, 8, 0, 0},
-    {128, 1, 8, 0, 0},
+    {128, 1, 8, 0, 0}, {4, 64, 8, 2, 0},  {8, 32, 8, 2, 0},  {4, 64, 4, 2, 0},
 };
 
 int fs_tune_count(void) { return (int)(sizeof(k_tune_order) / sizeof(k_tune_order[0])); }

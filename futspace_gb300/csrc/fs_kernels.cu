@@ -27,33 +27,19 @@ extern "C" int fsk_segmin_h1(const FsLaunch *, const FsTune *, int, cudaStream_t
 
 namespace {
 
-/* Per depth k (z = z_{k+1}): get_zs (fut/voxel_renderer.fut:34), get_h_line
- * (:43-60) and inv_z = (1/z) * scale (:217). The reference evaluates these once
- * per depth slice in its outer map (:215-217); so does this table. */
+/* The depth table of one view (DepthLine per depth), then FS_ZPAD zero entries. */
 __device__ __forceinline__ void ztable_fill(const FsView *Vp, float4 *zline, float *zinvz) {
   const int n = Vp->n;
-  const float d = Vp->d, z0 = Vp->z0, s = Vp->sa, c = Vp->ca, v = Vp->fov;
-  const float fw = (float)Vp->W;
-  const float a1 = fs(-c, fm(s, v)); /* left_x / z  */
-  const float a2 = fs(s, fm(c, v));  /* left_y / z  */
-  const float a3 = fs(c, fm(s, v));  /* right_x / z */
-  const float a4 = fs(-s, fm(c, v)); /* right_y / z */
+  const DepthLine dl(*Vp);
   float4 *zl = zline + Vp->zoff;
   float *zi = zinvz + Vp->zoff;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n + FS_ZPAD;
        k += gridDim.x * blockDim.x) {
-    if (k >= n) {
-      zl[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-      zi[k] = 0.0f;
-      continue;
-    }
-    const float fi = (float)(k + 1);
-    const float z = fm(fd(fi, 2.0f), fa(fm(2.0f, z0), fm(fs(fi, 1.0f), d)));
-    const float lx = fm(a1, z), ly = fm(a2, z), rx = fm(a3, z), ry = fm(a4, z);
-    const float dx = fd(fs(rx, lx), fw);
-    const float dy = fd(fs(ry, ly), fw);
-    zl[k] = make_float4(fa(lx, Vp->cam_x), fa(ly, Vp->cam_y), dx, dy);
-    zi[k] = fm(fd(1.0f, z), Vp->scale);
+    float4 L = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    float iz = 0.0f;
+    if (k < n) dl.entry(k, L, iz);
+    zl[k] = L;
+    zi[k] = iz;
   }
 }
 
@@ -175,14 +161,24 @@ extern "C" int fsk_tune_supported(const FsTune *t) {
   if (t->tw == TW_ && t->lc == LC_ && t->u == U_ && t->stage == STG_ && t->smooth == SM_ && \
       t->fx == FX_)                                                                         \
     return 1;
+#define FS_CASE_C(TW_, TPC_, U_)                                                      \
+  if (t->stage == 2 && t->tw == TW_ && t->lc == TPC_ && t->u == U_ && !t->smooth && !t->fx) \
+    return 1;
   FS_TUNE_LIST(FS_CASE)
   FS_TUNE_LIST_MODES(FS_CASE_M)
+  FS_COOP_LIST(FS_CASE_C)
 #undef FS_CASE
 #undef FS_CASE_M
+#undef FS_CASE_C
   return 0;
 }
 
 extern "C" size_t fsk_render_smem(const FsTune *t, int32_t stride_max) {
+#define FS_COOP_SMEM(TW_, TPC_, U_)                                  \
+  if (t->stage == 2 && t->tw == TW_ && t->lc == TPC_ && t->u == U_) \
+    return CoopShape<TW_, TPC_, U_>::fixed_bytes + CoopShape<TW_, TPC_, U_>::stage_bytes(stride_max);
+  FS_COOP_LIST(FS_COOP_SMEM)
+#undef FS_COOP_SMEM
   /* must match RenderShape<...>::fixed_bytes + stage */
   const size_t nw = (size_t)t->tw * t->lc / 32;
   const size_t box = t->stage ? 2ull * kBoxRows * t->tw * 4 : 0;
@@ -190,8 +186,8 @@ extern "C" size_t fsk_render_smem(const FsTune *t, int32_t stride_max) {
   return box + nw * queue_cap(t->u) * 8 * (t->smooth ? 2 : 1) + 256 * 4 + stage;
 }
 
-/* Screen columns per work item: a CTA tile with the shared-memory stage, a
- * warp strip with direct painting. */
+/* Screen columns per work item: a CTA tile with the shared-memory stage (and
+ * the cooperative tile), a warp strip with direct painting. */
 extern "C" int32_t fsk_item_width(const FsTune *t) { return t->stage ? t->tw : 32 / t->lc; }
 
 /* Work items one CTA takes at a time (warps per CTA with direct painting). */

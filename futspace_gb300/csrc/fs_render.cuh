@@ -59,6 +59,32 @@ __device__ __forceinline__ unsigned long long pack_event(int k, int col, int row
          ((unsigned long long)(uint32_t)row << 16) | (unsigned long long)(uint32_t)prev;
 }
 
+/* Depth-table entry of depth k (z = z_{k+1}) of one view: get_zs
+ * (fut/voxel_renderer.fut:34), get_h_line (:43-60) and inv_z = (1/z) * scale
+ * (:217), which the reference evaluates once per depth slice in its outer map
+ * (:215-217). L = {left_x + cam_x, left_y + cam_y, dx, dy}. */
+struct DepthLine {
+  float a1, a2, a3, a4, fw, d, z0, cam_x, cam_y, scale;
+  __device__ __forceinline__ explicit DepthLine(const FsView &V)
+      : a1(fs(-V.ca, fm(V.sa, V.fov))), /* left_x / z  */
+        a2(fs(V.sa, fm(V.ca, V.fov))),  /* left_y / z  */
+        a3(fs(V.ca, fm(V.sa, V.fov))),  /* right_x / z */
+        a4(fs(-V.sa, fm(V.ca, V.fov))), /* right_y / z */
+        fw((float)V.W),
+        d(V.d),
+        z0(V.z0),
+        cam_x(V.cam_x),
+        cam_y(V.cam_y),
+        scale(V.scale) {}
+  __device__ __forceinline__ void entry(int k, float4 &L, float &iz) const {
+    const float fi = (float)(k + 1);
+    const float z = fm(fd(fi, 2.0f), fa(fm(2.0f, z0), fm(fs(fi, 1.0f), d)));
+    const float lx = fm(a1, z), ly = fm(a2, z), rx = fm(a3, z), ry = fm(a4, z);
+    L = make_float4(fa(lx, cam_x), fa(ly, cam_y), fd(fs(rx, lx), fw), fd(fs(ry, ly), fw));
+    iz = fm(fd(1.0f, z), scale);
+  }
+};
+
 __device__ __forceinline__ void fence_proxy_async_shared() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
@@ -194,11 +220,9 @@ __device__ __forceinline__ void segment_range(const FsView *Vp, int seg, int &k_
  * bilinear in (column, depth along the view line), so the four corner samples
  * bound the box. A chunk whose bound is not above any of the strip's running
  * minima holds no event. (Power-of-two maps with a max pyramid only.) */
-__device__ __forceinline__ int chunk_row_bound(const FsMapDev &M, const float4 *zl,
-                                               const float *zi, float cam_h, float horizon,
-                                               int H, float cf, float cl, int ka, int kb) {
-  const float4 La = __ldg(zl + ka), Lb = __ldg(zl + kb);
-  const float iza = __ldg(zi + ka), izb = __ldg(zi + kb);
+__device__ __forceinline__ int box_row_bound(const FsMapDev &M, float4 La, float iza, float4 Lb,
+                                             float izb, float cam_h, float horizon, int H,
+                                             float cf, float cl) {
   const float2 a0 = axpy2(cf, make_float2(La.z, La.w), make_float2(La.x, La.y));
   const float2 a1 = axpy2(cl, make_float2(La.z, La.w), make_float2(La.x, La.y));
   const float2 b0 = axpy2(cf, make_float2(Lb.z, Lb.w), make_float2(Lb.x, Lb.y));
@@ -211,6 +235,14 @@ __device__ __forceinline__ int chunk_row_bound(const FsMapDev &M, const float4 *
   const int ra = min(max(f2i(fa(fm(dh, iza), horizon)), 0), H);
   const int rb = min(max(f2i(fa(fm(dh, izb), horizon)), 0), H);
   return min(ra, rb);
+}
+
+/* The same bound for depths [ka, kb] of a view's depth table. */
+__device__ __forceinline__ int chunk_row_bound(const FsMapDev &M, const float4 *zl,
+                                               const float *zi, float cam_h, float horizon,
+                                               int H, float cf, float cl, int ka, int kb) {
+  return box_row_bound(M, __ldg(zl + ka), __ldg(zi + ka), __ldg(zl + kb), __ldg(zi + kb), cam_h,
+                       horizon, H, cf, cl);
 }
 
 /* Skip bounds of 32 chunks at a time: lane j holds the bound of the chunk
@@ -485,6 +517,46 @@ __device__ __forceinline__ void render_strip(const FsLaunch &P, const FsView *Vp
   gapcols = gapbits;
 }
 
+/* Writes the stage's TW columns (rows [0, H)) to the frame: transposed
+ * through the two row-major box buffers and stored with TMA, or with plain
+ * stores when the frame has no tensor map. Ends with a barrier after every
+ * bulk store has read its box, so the stage and the boxes are free again. */
+template <int TW, int NT>
+__device__ __forceinline__ void store_tile(const FsLaunch &P, const FsView *Vp, int c0,
+                                           const uint32_t *stage, uint32_t *box, int tid) {
+  const int W = Vp->W, H = Vp->H, stride = H | 1;
+  if (Vp->tmap >= 0) {
+    const CUtensorMap *tm = P.views ? P.tmaps + Vp->tmap : &P.tmap0;
+    const int nb = (H + kBoxRows - 1) / kBoxRows;
+    for (int b = 0; b < nb; b++) {
+      uint32_t *buf = box + (b & 1) * kBoxRows * TW;
+      if (b >= 2) {
+        if (tid == 0) bulk_wait_read<1>();
+        __syncthreads();
+      }
+      for (int e = tid; e < kBoxRows * TW; e += NT) {
+        const int rr = e / TW, cc = e - rr * TW;
+        const int y = b * kBoxRows + rr;
+        buf[e] = (y < H) ? stage[cc * stride + y] : 0u;
+      }
+      fence_proxy_async_shared();
+      __syncthreads();
+      if (tid == 0) {
+        tma_store_2d(tm, buf, c0, b * kBoxRows);
+        bulk_commit();
+      }
+    }
+    if (tid == 0) bulk_wait_read<0>();
+  } else {
+    uint32_t *const out = Vp->out;
+    for (int e = tid; e < H * TW; e += NT) {
+      const int y = e / TW, cc = e - y * TW;
+      if (c0 + cc < W) __stcs(out + (size_t)y * W + c0 + cc, stage[cc * stride + y]);
+    }
+  }
+  __syncthreads();
+}
+
 /* The view, depth segment and first column of work item `item`. */
 template <int IW>
 __device__ __forceinline__ const FsView *decode_item(const FsLaunch &P, int item, int &seg,
@@ -563,36 +635,7 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
         if (c0 + lcl < W) fill_column([sc](int y) { return sc + y; }, 0, H, mf, gap, sky, lane);
       }
       __syncthreads();
-      if (Vp->tmap >= 0) {
-        const CUtensorMap *tm = P.views ? P.tmaps + Vp->tmap : &P.tmap0;
-        const int nb = (H + kBoxRows - 1) / kBoxRows;
-        for (int b = 0; b < nb; b++) {
-          uint32_t *buf = box + (b & 1) * kBoxRows * TW;
-          if (b >= 2) {
-            if (tid == 0) bulk_wait_read<1>();
-            __syncthreads();
-          }
-          for (int e = tid; e < kBoxRows * TW; e += NT) {
-            const int rr = e / TW, cc = e - rr * TW;
-            const int y = b * kBoxRows + rr;
-            buf[e] = (y < H) ? stage[cc * stride + y] : 0u;
-          }
-          fence_proxy_async_shared();
-          __syncthreads();
-          if (tid == 0) {
-            tma_store_2d(tm, buf, c0, b * kBoxRows);
-            bulk_commit();
-          }
-        }
-        if (tid == 0) bulk_wait_read<0>();
-      } else {
-        uint32_t *const out = Vp->out;
-        for (int e = tid; e < H * TW; e += NT) {
-          const int y = e / TW, cc = e - y * TW;
-          if (c0 + cc < W) __stcs(out + (size_t)y * W + c0 + cc, stage[cc * stride + y]);
-        }
-      }
-      __syncthreads();
+      store_tile<TW, NT>(P, Vp, c0, stage, box, tid);
     }
     if (tid == 0) bulk_wait_all();
   } else {
@@ -736,7 +779,309 @@ __global__ void __launch_bounds__(TW *LC, 1024 / (TW * LC)) segmin_kernel(
   }
 }
 
+/* ---- the cooperative tile form (stage 2) -------------------------------------
+ * A CTA renders a tile of TW columns with TPC threads per column, marching the
+ * depths in blocks of NB = TPC * U: thread (c, j) of the tile takes the U
+ * consecutive depths j*U .. j*U + U-1 of each block for column c. Per block b:
+ *  A. every thread computes the rows of its U samples at once (all gathers in
+ *     flight), unless a max-pyramid bound over its warp's columns and depths
+ *     shows that none can be below the column minima at the block's start;
+ *  B. the running minimum before each sample comes from a min-scan over the
+ *     column's threads: the thread's own U rows, a warp scan (__shfl_up_sync
+ *     in steps of TW lanes) and the warp totals in shared memory; events (row
+ *     below that minimum) go to the block's list;
+ *  C. all warps colour the listed events and write each colour at its event's
+ *     row of the stage, which starts the tile filled with the gap value: this
+ *     is the reference's scatter (fut/voxel_renderer.fut:244); its forward fill
+ *     (:246) runs once over the finished tile.
+ * Phases C of block b-1 and A of block b run together, and block b+1's
+ * depth-table entries load during B of block b (two buffers each), so a block
+ * costs two barriers and its colour gathers overlap the next block's height
+ * gathers. The column chain is one block per step instead of one chunk, so a
+ * single frame with few columns keeps every SM busy. After the last block (or
+ * once every column's minimum is row 0) the tile gets the forward fill and
+ * sky. The stage is row-major, so every 32-row box of the tile goes to the
+ * frame straight from it with TMA, all boxes back to back. */
+template <int TW, int TPC, int U>
+struct CoopShape {
+  static constexpr int NT = TW * TPC;
+  static constexpr int NW = NT / 32;
+  static constexpr int NB = TPC * U;   /* depths per block */
+  static constexpr int ECAP = TW * NB; /* events per block: at most one per sample */
+  static constexpr size_t lut_bytes = 256 * 4;
+  static constexpr size_t zl_bytes = 2ull * NB * 16; /* two blocks' entries */
+  static constexpr size_t zi_bytes = 2ull * NB * 4;
+  static constexpr size_t ev_bytes = 2ull * ECAP * 4; /* two blocks' event lists */
+  /* warp totals [NW][TW], block-start minima [2][TW], event counts [2], item */
+  static constexpr size_t misc_bytes = ((size_t)NW * TW + 2 * TW + 3) * 4;
+  /* the stage starts on a 128-byte boundary, as do its boxes (TMA sources) */
+  static constexpr size_t fixed_bytes =
+      (lut_bytes + zl_bytes + zi_bytes + ev_bytes + misc_bytes + 127) / 128 * 128;
+  static constexpr int min_blocks = NT >= 1024 ? 1 : 1024 / NT;
+  /* the stage: row-major [H rounded up to whole boxes][TW] */
+  static __host__ __device__ constexpr size_t stage_bytes(int H) {
+    return (size_t)TW * (size_t)((H + kBoxRows - 1) / kBoxRows * kBoxRows) * 4;
+  }
+};
+
+/* Writes a row-major [rows][TW] stage to the frame: every 32-row box straight
+ * from the stage with TMA (no copy, no wait between boxes), or with plain
+ * stores when the frame has no tensor map. Ends with a barrier after the bulk
+ * stores have read the stage. */
+template <int TW, int NT>
+__device__ __forceinline__ void store_rows(const FsLaunch &P, const FsView *Vp, int c0,
+                                           const uint32_t *stage, int tid) {
+  const int W = Vp->W, H = Vp->H;
+  if (Vp->tmap >= 0) {
+    fence_proxy_async_shared();
+    __syncthreads();
+    if (tid == 0) {
+      const CUtensorMap *tm = P.views ? P.tmaps + Vp->tmap : &P.tmap0;
+      for (int b = 0; b * kBoxRows < H; b++)
+        tma_store_2d(tm, stage + b * kBoxRows * TW, c0, b * kBoxRows);
+      bulk_commit();
+      bulk_wait_read<0>();
+    }
+  } else {
+    __syncthreads();
+    uint32_t *const out = Vp->out;
+    for (int e = tid; e < H * TW; e += NT) {
+      const int y = e / TW, cc = e - y * TW;
+      if (c0 + cc < W) __stcs(out + (size_t)y * W + c0 + cc, stage[e]);
+    }
+  }
+  __syncthreads();
+}
+
+/* Event list entry of the cooperative tile: depth within the block (11 bits),
+ * tile column (5), row (16). */
+__device__ __forceinline__ uint32_t pack_coop_event(int kl, int c, int row) {
+  return ((uint32_t)kl << 21) | ((uint32_t)c << 16) | (uint32_t)row;
+}
+
+template <int TW, int TPC, int U, int HF, int CF>
+__global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
+    coop_kernel(const __grid_constant__ FsLaunch P) {
+  using S = CoopShape<TW, TPC, U>;
+  constexpr int NT = S::NT, NW = S::NW, NB = S::NB, ECAP = S::ECAP;
+  static_assert(TW >= 4 && 32 % TW == 0 && NT % 32 == 0, "a warp holds whole runs of TW columns");
+  static_assert(NB <= 2048 && TW <= 32, "event fields");
+
+  extern __shared__ __align__(1024) unsigned char smem[];
+  float *lut = reinterpret_cast<float *>(smem);
+  float4 *zt = reinterpret_cast<float4 *>(smem + S::lut_bytes);
+  float *zv = reinterpret_cast<float *>(smem + S::lut_bytes + S::zl_bytes);
+  uint32_t *evq = reinterpret_cast<uint32_t *>(smem + S::lut_bytes + S::zl_bytes + S::zi_bytes);
+  int *wtot =
+      reinterpret_cast<int *>(smem + S::lut_bytes + S::zl_bytes + S::zi_bytes + S::ev_bytes);
+  int *mcol = wtot + NW * TW;
+  int *scal = mcol + 2 * TW; /* [0], [1] events of the even / odd block, [2] next item */
+  uint32_t *stage = reinterpret_cast<uint32_t *>(smem + S::fixed_bytes);
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int c = tid % TW; /* the thread's column within the tile (lane % TW) */
+  const int j = tid / TW; /* its run within each depth block */
+  for (int i = tid; i < 256; i += NT) lut[i] = __fdiv_rn((float)i, 255.0f);
+  const LutChannels chan{lut};
+  uint32_t n_samples = 0, n_events = 0;
+
+  for (int iter = 0;; iter++) {
+    int item;
+    if (P.head) {
+      if (tid == 0) scal[2] = atomicAdd(P.head, 1);
+      __syncthreads();
+      item = scal[2];
+    } else {
+      item = iter == 0 ? (int)blockIdx.x : P.nitems;
+    }
+    if (item >= P.nitems) break;
+    int seg, c0;
+    const FsView *Vp = decode_item<TW>(P, item, seg, c0);
+    const int W = Vp->W, H = Vp->H, n = Vp->n;
+    const uint32_t sky = Vp->sky, gap = Vp->gap;
+    const FsMapDev &M = P.maps[Vp->map];
+    const HeightMap hmap{M.q, M.MW, M.MH};
+    const bool p2 = M.pow2 != 0;
+    const float cam_h = Vp->cam_h, horizon = Vp->horizon;
+    const float fcol = (float)(c0 + c);
+    const float4 *zl = P.zline + Vp->zoff;
+    const float *zi = P.zinvz + Vp->zoff;
+
+    /* depth-table entries of block kb into buffer half: position p holds
+     * depth kb + (p % TPC) * U + p / TPC, so step i of run j reads i*TPC + j */
+    auto load_table = [&](int kb, int half) {
+      for (int p = tid; p < NB; p += NT) {
+        const int e = (p % TPC) * U + p / TPC;
+        float4 L = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        float iz = 0.0f;
+        if (kb + e < n) {
+          L = __ldg(zl + kb + e);
+          iz = __ldg(zi + kb + e);
+        }
+        zt[half * NB + p] = L;
+        zv[half * NB + p] = iz;
+      }
+    };
+    /* colour the events of the block in buffer half, each at its row */
+    auto colour_events = [&](int half) {
+      const int ne = scal[half];
+      if (P.stats && tid == 0) n_events += (uint32_t)ne;
+      for (int e = tid; e < ne; e += NT) {
+        const uint32_t ev = evq[half * ECAP + e];
+        const int kl = (int)(ev >> 21), ec = (int)((ev >> 16) & 31u), er = (int)(ev & 0xFFFFu);
+        const float4 L = zt[half * NB + (kl % U) * TPC + kl / U];
+        const float2 xy =
+            axpy2((float)(c0 + ec), make_float2(L.z, L.w), make_float2(L.x, L.y));
+        stage[er * TW + ec] =
+            CF ? color_bilinear(M, chan, xy.x, xy.y) : color_nearest(M, xy.x, xy.y);
+      }
+    };
+
+    /* a column past the frame's right edge starts (and stays) at row 0 */
+    if (tid < TW) mcol[tid] = (c0 + tid < W) ? H : 0;
+    if (tid == 0) scal[0] = scal[1] = 0;
+    for (int e = tid; e < H * TW; e += NT) stage[e] = gap;
+    load_table(0, 0);
+    __syncthreads();
+
+    int fin = 1; /* which half of mcol holds the minima after the last block */
+    for (int kb = 0, par = 0;; kb += NB, par ^= 1) {
+      /* X: rows of block kb (A) with the colours of the previous block (C) */
+      const int mstart = mcol[par * TW + c];
+      int r[U];
+#pragma unroll
+      for (int i = 0; i < U; i++) r[i] = H;
+      const float4 *ztb = zt + par * NB;
+      const float *zvb = zv + par * NB;
+      /* the warp's depths [ka, kz] over its TW columns */
+      const int jw = warp * (32 / TW);
+      const int ka = kb + jw * U, kz = min(kb + (jw + 32 / TW) * U, n) - 1;
+      bool skip = ka > kz || __all_sync(FS_FULL_MASK, mstart == 0);
+      if (!skip && M.pyr) {
+        const int ea = ka - kb, ez = kz - kb;
+        const int pa = (ea % U) * TPC + ea / U, pz = (ez % U) * TPC + ez / U;
+        const int b = box_row_bound(M, ztb[pa], zvb[pa], ztb[pz], zvb[pz], cam_h, horizon, H,
+                                    (float)c0, (float)max(c0, min(c0 + TW, W) - 1));
+        skip = b >= (int)__reduce_max_sync(FS_FULL_MASK, (unsigned)mstart);
+      }
+      if (!skip && mstart > 0) {
+        auto rows = [&](auto p2tag) {
+          constexpr bool P2 = decltype(p2tag)::value;
+#pragma unroll
+          for (int i = 0; i < U; i++) {
+            const float4 L = ztb[i * TPC + j];
+            const float2 xy = axpy2(fcol, make_float2(L.z, L.w), make_float2(L.x, L.y));
+            const float hh = HF ? height_bilinear<P2>(hmap, xy.x, xy.y)
+                                : height_nearest<P2>(hmap, xy.x, xy.y);
+            const int rr = min(max(f2i(fa(fm(fs(cam_h, hh), zvb[i * TPC + j]), horizon)), 0), H);
+            r[i] = (kb + j * U + i < n) ? rr : H;
+          }
+        };
+        if (p2)
+          rows(BoolTag<true>{});
+        else
+          rows(BoolTag<false>{});
+        if (P.stats) n_samples += (uint32_t)max(0, min(U, n - kb - j * U));
+      }
+      if (kb > 0) colour_events(par ^ 1);
+      int run = H;
+#pragma unroll
+      for (int i = 0; i < U; i++) run = min(run, r[i]);
+      int incl = run;
+#pragma unroll
+      for (int off = TW; off < 32; off <<= 1) {
+        const int t = __shfl_up_sync(FS_FULL_MASK, incl, off);
+        if (lane >= off) incl = min(incl, t);
+      }
+      const int ex = __shfl_up_sync(FS_FULL_MASK, incl, TW);
+      if (lane >= 32 - TW) wtot[warp * TW + c] = incl;
+      __syncthreads();
+
+      /* Y: the minimum before each sample, the block's events (B), and the
+       * next block's depth-table entries */
+      int prev = mstart;
+      for (int w = 0; w < warp; w++) prev = min(prev, wtot[w * TW + c]);
+      if (lane >= TW) prev = min(prev, ex);
+      if (j == TPC - 1) mcol[(par ^ 1) * TW + c] = min(prev, run);
+      int cnt = 0;
+      {
+        int pv = prev;
+#pragma unroll
+        for (int i = 0; i < U; i++)
+          if (r[i] < pv) {
+            cnt++;
+            pv = r[i];
+          }
+      }
+      int csum = cnt;
+#pragma unroll
+      for (int off = 1; off < 32; off <<= 1) {
+        const int t = __shfl_up_sync(FS_FULL_MASK, csum, off);
+        if (lane >= off) csum += t;
+      }
+      int base = 0;
+      if (lane == 31 && csum) base = atomicAdd(&scal[par], csum);
+      base = __shfl_sync(FS_FULL_MASK, base, 31) + csum - cnt;
+      if (cnt) {
+        uint32_t *q = evq + par * ECAP;
+#pragma unroll
+        for (int i = 0; i < U; i++)
+          if (r[i] < prev) {
+            q[base++] = pack_coop_event(j * U + i, c, r[i]);
+            prev = r[i];
+          }
+      }
+      const bool more = kb + NB < n;
+      if (more) load_table(kb + NB, par ^ 1);
+      if (tid == 0) scal[par ^ 1] = 0; /* the previous block's list is coloured */
+      __syncthreads();
+
+      /* the last block, or every column at row 0: colour it and finish */
+      bool done = !more;
+      if (more) {
+        bool all0 = true;
+#pragma unroll
+        for (int cc = 0; cc < TW; cc++) all0 = all0 && mcol[(par ^ 1) * TW + cc] == 0;
+        done = all0;
+      }
+      if (done) {
+        colour_events(par);
+        fin = par ^ 1;
+        break;
+      }
+    }
+    __syncthreads();
+
+    /* forward fill + sky per column (a warp per column), then the tile store */
+    for (int cc = warp; cc < TW; cc += NW) {
+      const int mf = mcol[fin * TW + cc];
+      uint32_t *sc = stage + cc;
+      if (c0 + cc < W)
+        fill_column([sc](int y) { return sc + y * TW; }, 0, H, mf, gap, sky, lane);
+    }
+    store_rows<TW, NT>(P, Vp, c0, stage, tid);
+  }
+  if (tid == 0) bulk_wait_all();
+  if (P.stats) {
+    unsigned long long ns = n_samples, ne = n_events;
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) ns += __shfl_down_sync(FS_FULL_MASK, ns, off);
+    if (lane == 0) {
+      atomicAdd(reinterpret_cast<unsigned long long *>(P.stats), ns);
+      if (tid == 0) atomicAdd(reinterpret_cast<unsigned long long *>(P.stats) + 1, ne);
+    }
+  }
+}
+
 }  // namespace fsd
+
+/* Cooperative tile configurations (TW, threads per column, depths per thread
+ * per block), stage 2 of the tuning tuple. */
+#define FS_COOP_LIST(X) \
+  X(8, 64, 8)           \
+  X(4, 64, 8)           \
+  X(8, 32, 8)           \
+  X(4, 64, 4)
 
 /* Kernel modes beyond the plain render, each compiled for a few configurations
  * and every filter pair: (TW, LC, U, STG, smoothing, epilogue). The epilogue

@@ -1,6 +1,6 @@
 /*
- * Instantiates the render kernel for one (height filter, colour filter) pair
- * and every configuration of FS_TUNE_LIST and FS_TUNE_LIST_MODES. Included by fs_render_h?c?.cu with
+ * Instantiates the render kernels for one (height filter, colour filter) pair:
+ * every configuration of FS_TUNE_LIST, FS_TUNE_LIST_MODES and FS_COOP_LIST. Included by fs_render_h?c?.cu with
  * FS_HF, FS_CF and FS_RENDER_ENTRY defined, so the four pairs compile as
  * separate translation units in parallel.
  *
@@ -39,6 +39,23 @@ extern "C" int FS_RENDER_ENTRY(int op, const FsLaunch *L, const FsTune *t, int g
 #undef FS_CASE
 #undef FS_CASE_M
 #undef FS_CASE_S
+/* the cooperative tile form (plain mode only) */
+#define FS_COOP_CASE(TW_, TPC_, U_)                                                          \
+  if (t->stage == 2 && t->tw == TW_ && t->lc == TPC_ && t->u == U_ && !t->smooth && !t->fx) { \
+    static int smem_set[64];                                                               \
+    auto kern = fsd::coop_kernel<TW_, TPC_, U_, FS_HF, FS_CF>;                             \
+    if (smem_set[dev] < (int)smem) {                                                       \
+      e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+      if (e != cudaSuccess) return (int)e;                                                 \
+      smem_set[dev] = (int)smem;                                                           \
+    }                                                                                      \
+    if (op == 1) return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern,      \
+                                                                           TW_ * TPC_, smem); \
+    kern<<<grid, TW_ * TPC_, smem, st>>>(*L);                                              \
+    return (int)cudaGetLastError();                                                        \
+  }
+  FS_COOP_LIST(FS_COOP_CASE)
+#undef FS_COOP_CASE
   return (int)cudaErrorInvalidValue;
 }
 

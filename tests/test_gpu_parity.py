@@ -341,3 +341,75 @@ def test_degenerate_screen_sizes(fs, orc, gpu_ctx, maps256):
     plan.run()
     for (w, h), f in zip(sizes, plan.frames()):
         assert count_diff(f, _oracle(orc, cam, p, hm, cm, w, h)) == 0, (w, h)
+
+
+@pytest.mark.parametrize("hf,cf", FILTERS)
+def test_cooperative_tile_exact(fs, orc, gpu_ctx, maps256, hf, cf):
+    """The cooperative tile form (stage 2: a CTA marches all depth blocks of its
+    columns at once, min-scan across threads) on adversarial cameras (below and
+    at the terrain: every column reaches row 0 early), a non-power-of-two map,
+    degenerate and odd screen sizes, both gap rules and the mode-B schedule."""
+    hm, cm = maps256
+    cm = cm.copy()
+    cm[::3, ::2] = 0
+    fmap = fs.Map(gpu_ctx, hm, cm)
+    hn = fs.gen_heights(3, 512, 0.6)[:300, :200].copy()
+    cn = fs.gen_colors(4, hn, 12)
+    fmap_n = fs.Map(gpu_ctx, hn, cn)
+    at = orc.lib().fso_height_bilinear(hm.ctypes.data, 256, 256, 64.5, 64.25)
+    cams = [fs.Camera(100.0, 100.0, 300.0, 0.0, 24.0, 200.0, 1.2, 0xFF9090E0),
+            fs.Camera(-37.0, -300.0, 120.0, 1.5707964, 30.0, 400.0, 1.2, 0xFF9090E0),
+            fs.Camera(64.5, 64.25, -10.0, 0.3, 24.0, 150.0, 1.2, 0xFF9090E0),
+            fs.Camera(64.5, 64.25, at, 0.3, 24.0, 150.0, 1.2, 0xFF9090E0)]
+    cams += fs.gen_cameras(161, hm, 2, above=(20, 90), distance=(400, 1500), screen_h=96)
+    coop = [t for t in fs.tune_table() if t[3] == 2]
+    assert coop
+    try:
+        for tune in coop:
+            gpu_ctx.force_tune(tune)
+            for gap in (0, 1):
+                p = fs.default_params(height_filter=hf, color_filter=cf, gap_rule=gap)
+                for cam in cams:
+                    for w, h in ((61, 47), (128, 96), (1, 1), (3, 300), (300, 3)):
+                        got = gpu_ctx.render(fmap, cam, w, h, params=p)
+                        ref = _oracle(orc, cam, p, hm, cm, w, h)
+                        assert count_diff(got, ref) == 0, (tune, gap, w, h)
+            p = fs.default_params(height_filter=hf, color_filter=cf)
+            for cam in fs.gen_cameras(9, hn, 2, above=(30, 60), distance=(300, 700),
+                                      screen_h=90):
+                got = gpu_ctx.render(fmap_n, cam, 120, 90, params=p)
+                assert count_diff(got, _oracle(orc, cam, p, hn, cn, 120, 90)) == 0, tune
+            pb = fs.default_params(invz_param1=0.005, invz_param2=1.0, magic_number=240.0,
+                                   height_filter=hf, color_filter=cf, gap_rule=1, floor_n=0)
+            cam = fs.Camera(128.0, 200.0, 78.0, 0.0, 100.0, 800.0, 1.0, 0xFF9090E0)
+            got = gpu_ctx.render(fmap, cam, 800, 400, params=pb)
+            assert count_diff(got, _oracle(orc, cam, pb, hm, cm, 800, 400)) == 0, tune
+    finally:
+        gpu_ctx.force_tune(None)
+
+
+def test_cooperative_tile_1080p_frame(fs, orc, gpu_ctx):
+    """A 1920x1080 frame over 4096^2 maps at D=3000 (2449 depths: several depth
+    blocks per tile) through every cooperative configuration, alone and in a
+    batch plan."""
+    hm = fs.gen_heights(7, 4096, 0.55)
+    cm = fs.gen_colors(8, hm, 12)
+    fmap = fs.Map(gpu_ctx, hm, cm)
+    walk = fs.gen_walk(9, hm, 3, step=2.0, yaw=0.02, above=(30, 120), distance=3000.0,
+                       screen_h=1080)
+    p = fs.default_params()
+    refs = [_oracle(orc, c, p, hm, cm, 1920, 1080) for c in walk]
+    coop = [t for t in fs.tune_table() if t[3] == 2]
+    try:
+        for tune in coop:
+            gpu_ctx.force_tune(tune)
+            for c, ref in zip(walk, refs):
+                assert count_diff(gpu_ctx.render(fmap, c, 1920, 1080), ref) == 0, tune
+    finally:
+        gpu_ctx.force_tune(None)
+    plan = fs.Plan(gpu_ctx, [fmap], [(c, 1920, 1080) for c in walk])
+    for tune in coop:
+        plan.set_tune(*tune)
+        plan.run()
+        bad = [i for i, (f, r) in enumerate(zip(plan.frames(), refs)) if count_diff(f, r)]
+        assert not bad, (tune, bad)
