@@ -36,6 +36,11 @@ RESOLUTIONS = [(320, 240), (640, 480), (1280, 720), (1920, 1080), (2560, 1440)]
 MAP_SEED_H, MAP_SEED_C, VIEW_SEED = 7, 8, 20240601
 # the metric both arms report (Gpix/s = total frame pixels / time)
 METRIC = "Gpix/s (bit-exact voxel-space frames), batched multi-view"
+METRIC_SINGLE = "Gpix/s (bit-exact voxel-space frames), one 1920x1080 frame per plain call"
+
+
+def metric_for(workload: str) -> str:
+    return METRIC_SINGLE if workload == "single1080" else METRIC
 
 
 def batch_views(fs, hm, nviews: int, seed: int):
@@ -86,6 +91,14 @@ def make_workload(fs, name: str, rank: int):
         return hm, cm, walk_views(fs, hm, 9 + rank), {
             "workload": "walk1080: 64-frame walk, 1920x1080, D=3000, 4096^2 maps",
             "views": 64, "map": "4096x4096 u8 heights + u32 colours"}
+    if name == "single1080":
+        hm = fs.gen_heights(MAP_SEED_H, 4096, 0.55)
+        cm = fs.gen_colors(MAP_SEED_C, hm, 12)
+        return hm, cm, walk_views(fs, hm, 9 + rank), {
+            "workload": "single1080: one 1920x1080 frame per step through the plain per-frame "
+                        "call (fs_render_device), cameras of the 64-frame walk in turn, D=3000, "
+                        "4096^2 maps",
+            "views": 1, "map": "4096x4096 u8 heights + u32 colours"}
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -165,18 +178,24 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def profiled_traffic(name: str):
-    """DRAM bytes per launch from the committed ncu summary, if one exists."""
+def profiled_value(name: str, key: str):
+    """A per-launch figure (`key: value` line) from the committed ncu summary
+    of workload `name`, if one exists."""
     p = ROOT / "profiles" / f"render_{name}.md"
     if not p.exists():
         return None
     for line in p.read_text().splitlines():
-        if line.startswith("dram_bytes_per_launch:"):
+        if line.startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
                 return None
     return None
+
+
+def profiled_traffic(name: str):
+    """DRAM bytes per launch from the committed ncu summary, if one exists."""
+    return profiled_value(name, "dram_bytes_per_launch")
 
 
 def cpu_reference_rate(views, hm, cm, max_seconds: float, threads: int, params=None):
@@ -209,7 +228,8 @@ def run_reference(args, rank: int, world: int):
     for step in range(args.warmup + args.steps):
         # each step: a bounded sample of the workload (views in a rotating order)
         k = (step * 7) % len(views)
-        sample = [views[(k + i) % len(views)] for i in range(args.ref_views)]
+        nv = 1 if args.workload == "single1080" else args.ref_views
+        sample = [views[(k + i) % len(views)] for i in range(nv)]
         g, used, px, dt = cpu_reference_rate(sample, hm, cm, args.ref_seconds, threads, oparams)
         if step >= args.warmup:
             rates.append(g)
@@ -217,13 +237,14 @@ def run_reference(args, rank: int, world: int):
             dts += dt
     value = pxs / dts / 1e9
     line = {
-        "impl": "reference", "metric": METRIC, "value": value,
+        "impl": "reference", "metric": metric_for(args.workload), "value": value,
         "unit": "Gpix/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000.0 * dts / max(1, args.steps), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": cfg,
         "cpu_baseline": {"value": value, "unit": "Gpix/s", "cores": threads, "kind": "port",
-                         "sample": f"{args.ref_views} views per step of the {args.workload} "
+                         "sample": f"{1 if args.workload == 'single1080' else args.ref_views} "
+                                   f"views per step of the {args.workload} "
                                    "workload, CPU oracle (C restatement of the reference render, "
                                    "OpenMP over columns)"},
         "e2e": {"value": value, "unit": "Gpix/s", "h2d_bytes_per_step": 0,
@@ -313,6 +334,159 @@ def run_serve(args, rank: int, world: int):
         print(json.dumps(line), flush=True)
 
 
+def run_single(args, rank: int, world: int, local: int):
+    """One 1920x1080 frame per step through the plain per-frame call
+    (fs_render_device: depth-table kernel + render kernel), maps resident, L2
+    flushed between steps, the autotuned single-frame configuration."""
+    import torch
+    import futspace_gb300 as fs
+    from futspace_gb300 import replicas
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = f"cuda:{local}"
+    ctx = fs.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream_handle, device=local)
+    hm, cm, views, cfg = make_workload(fs, "single1080", rank)
+    fmap = fs.Map(ctx, hm, cm)
+    W, H = 1920, 1080
+    cams = [v[0] for v in views]
+    if args.tune:
+        tune, tune_ms = tuple(int(x) for x in args.tune.split(",")), None
+        ctx.force_tune(tune)
+    else:
+        tune, tune_ms = ctx.autotune_frame(fmap, cams[0], W, H, reps=5)
+    out = torch.empty(W * H, dtype=torch.int32, device=dev)
+    # work counters over the 64 cameras (untimed)
+    ctx.stats(True)
+    for c in cams:
+        ctx.render_device(fmap, c, W, H, out.data_ptr())
+    samples, events = ctx.stats(False)
+    samples /= len(cams)
+    events /= len(cams)
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device=dev)
+    ctx.set_option("time", 1)
+    for i in range(args.warmup):
+        ctx.render_device(fmap, cams[i % len(cams)], W, H, out.data_ptr())
+    ctx.sync()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = ctx.launches
+    t_step, t_kernel = [], []
+    for i in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(1)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        ctx.render_device(fmap, cams[i % len(cams)], W, H, out.data_ptr())
+        b.record(stream)
+        b.synchronize()
+        t_step.append(a.elapsed_time(b))
+        t_kernel.append(ctx.kernel_ms())
+    gpu_launches = ctx.launches - launches0
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ctx.set_option("time", 0)
+
+    # end to end through the C ABI with a host buffer: fs_render renders and
+    # copies the frame to pinned host memory, then waits for it
+    e2e = None
+    if not args.no_e2e:
+        host = fs.PinnedBuffer((H, W))
+        t_e2e = []
+        for i in range(args.warmup + args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(1)
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ctx.render(fmap, cams[i % len(cams)], W, H, out=host.array)
+            b.record(stream)
+            b.synchronize()
+            if i >= args.warmup:
+                t_e2e.append(a.elapsed_time(b))
+        e2e_ms = float(np.mean(t_e2e))
+        e2e = {"value": W * H / e2e_ms / 1e6, "unit": "Gpix/s",
+               # the camera travels in the launch parameters (one view record)
+               "h2d_bytes_per_step": 128, "d2h_bytes_per_step": 4 * W * H,
+               "ms_per_step": e2e_ms}
+        host.close()
+
+    ms = float(np.mean(t_step))
+    agg = replicas.aggregate(W * H, ms, dist=dist, device=dev)
+    k_ms = float(np.mean(t_kernel))
+    peaks = measured_peaks()
+    l2_gbs = max(ctx.measure_l2_read_gbs() for _ in range(3))
+    vb = {"frame": 4 * W * H, "height_gather": 4 * samples, "color_gather": 16 * events}
+    alg = vb["frame"] + vb["height_gather"] + vb["color_gather"]
+    achieved = alg / (k_ms * 1e-3) / 1e9
+    n = fs.num_depths(cams[0].distance)
+    # the gather/store roofline of one frame: the slower of the frame bytes at
+    # the HBM copy rate and the gathers' L2 read sectors (ncu, committed
+    # summary; else the algorithmic gather bytes) at the measured L2 read rate
+    sectors = profiled_value("single1080", "l2_read_sectors_per_launch")
+    gather_bytes = 32 * sectors if sectors else vb["height_gather"] + vb["color_gather"]
+    store_us = 4 * W * H / (peaks["hbm_gbs"] * 1e3)
+    gather_us = gather_bytes / (l2_gbs * 1e3)
+    bound_us = max(store_us, gather_us)
+
+    cpu = None
+    if rank == 0 and args.cpu_seconds > 0:
+        import oracle
+        threads = oracle.lib().fso_max_threads()
+        g, used, cpx, dt = cpu_reference_rate(views, hm, cm, args.cpu_seconds, threads)
+        cpu = {"value": g, "unit": "Gpix/s", "cores": threads, "kind": "port",
+               "sample": f"first {used} frames of the walk ({cpx} px, {dt:.1f} s), CPU oracle "
+                         "(C restatement of the reference render, OpenMP over columns)"}
+    if rank == 0:
+        line = {
+            "metric": METRIC_SINGLE,
+            "value": agg["gpix_s"], "unit": "Gpix/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": agg["ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded diamond-square maps and camera walk)",
+            "config": {**cfg, "l2": "flushed between timed steps (256 MB write)",
+                       "tune": {"tile_width": tune[0], "threads_or_lanes_per_column": tune[1],
+                                "depth_per_thread": tune[2], "stage": tune[3]},
+                       "autotune_ms": tune_ms},
+            "latency_ms": {"p50": float(np.percentile(t_step, 50)),
+                           "p99": float(np.percentile(t_step, 99))},
+            "frames_per_s": world / agg["ms"] * 1e3,
+            "work": {"depth_samples_per_frame": samples, "full_depth_samples": n * W,
+                     "events_coloured_per_frame": events},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"],
+                         "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                         "traffic": profiled_traffic("single1080"),
+                         "peak_source": peaks["source"],
+                         "kernel": "render kernel of one plain call", "kernel_ms": k_ms,
+                         "bytes_per_launch": vb},
+            "gather_store_roofline": {"store_us": store_us, "gather_us": gather_us,
+                                      "gather_bytes": gather_bytes,
+                                      "gather_bytes_source": "ncu L2 read sectors x 32"
+                                      if sectors else "algorithmic gather bytes",
+                                      "l2_read_gbs_measured": l2_gbs, "bound_us": bound_us,
+                                      "kernel_us": k_ms * 1e3,
+                                      "frac": bound_us / (k_ms * 1e3)},
+            "clocks": clk,
+            "e2e": e2e,
+            "gpu_launches": gpu_launches,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -320,7 +494,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batch512",
-                    choices=["batch512", "walk1080", "large4k", "serve"])
+                    choices=["batch512", "walk1080", "large4k", "single1080", "serve"])
     ap.add_argument("--serve-rates", default="1000,5000,10000,20000")
     ap.add_argument("--serve-seconds", type=float, default=2.0)
     ap.add_argument("--no-autotune", action="store_true")
@@ -345,6 +519,9 @@ def main():
         return
     if args.workload == "serve":
         run_serve(args, rank, world)
+        return
+    if args.workload == "single1080":
+        run_single(args, rank, world, local)
         return
 
     import torch

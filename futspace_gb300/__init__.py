@@ -137,6 +137,8 @@ def lib():
     _sig(L, "fs_ctx_get_stream", vp, [vp])
     _sig(L, "fs_ctx_kernel_launches", i64, [vp])
     _sig(L, "fs_ctx_stats", C.c_int, [vp, i32, P(u64)])
+    _sig(L, "fs_ctx_kernel_ms", C.c_int, [vp, P(C.c_float)])
+    _sig(L, "fs_measure_l2_read_gbs", C.c_int, [vp, i64, i32, P(C.c_float)])
     _sig(L, "fs_ctx_force_tune", C.c_int, [vp, P(i32)])
     _sig(L, "fs_ctx_set_option", C.c_int, [vp, C.c_char_p, i64])
     _sig(L, "fs_map_new", C.c_int, [vp, P(vp), vp, vp, i64, i64])
@@ -370,6 +372,18 @@ class Context:
         """tune = (tile_width, lanes_per_column, depth_per_lane, stage) or None."""
         t = (C.c_int32 * 5)(*(tuple(tune) + (0,) * (5 - len(tune)))) if tune else None
         self.check(lib().fs_ctx_force_tune(self._h, t), "force_tune")
+
+    def kernel_ms(self) -> float:
+        """Render-kernel device time of the last plain call made with option "time"."""
+        ms = C.c_float()
+        self.check(lib().fs_ctx_kernel_ms(self._h, C.byref(ms)), "kernel_ms")
+        return ms.value
+
+    def measure_l2_read_gbs(self, nbytes: int = 48 << 20, reps: int = 40) -> float:
+        """L2 read bandwidth (GB/s) of an L2-resident buffer (a roofline denominator)."""
+        gbs = C.c_float()
+        self.check(lib().fs_measure_l2_read_gbs(self._h, nbytes, reps, C.byref(gbs)), "l2 probe")
+        return gbs.value
 
     def stats(self, enable: bool = True):
         out = (C.c_uint64 * 2)()

@@ -204,6 +204,8 @@ void fs_ctx_free(fs_ctx *ctx) {
   cudaFree(ctx->frame_dev);
   cudaFree(ctx->segbuf);
   cudaFree(ctx->stats_dev);
+  if (ctx->ev_kernel[0]) cudaEventDestroy(ctx->ev_kernel[0]);
+  if (ctx->ev_kernel[1]) cudaEventDestroy(ctx->ev_kernel[1]);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
   free(ctx);
 }
@@ -234,6 +236,14 @@ int fs_ctx_set_option(fs_ctx *ctx, const char *name, int64_t value) {
     ctx->use_tma = (value && ctx->encode) ? 1 : 0;
   } else if (!strcmp(name, "split")) {
     ctx->no_split = value ? 0 : 1;
+  } else if (!strcmp(name, "time")) {
+    if (value && !ctx->ev_kernel[0]) {
+      cudaSetDevice(ctx->device);
+      if (cudaEventCreate(&ctx->ev_kernel[0]) || cudaEventCreate(&ctx->ev_kernel[1]))
+        return fs_fail(ctx, FS_ERR_CUDA, "cudaEventCreate(kernel timer)");
+    }
+    ctx->time_kernel = value ? 1 : 0;
+    ctx->kernel_timed = 0;
   } else {
     return fs_fail(ctx, FS_ERR_ARG, "unknown option '%s'", name);
   }
@@ -254,6 +264,56 @@ int fs_ctx_force_tune(fs_ctx *ctx, const int32_t tune5[5]) {
   }
   ctx->forced = t;
   return FS_OK;
+}
+
+int fs_ctx_kernel_ms(fs_ctx *ctx, float *ms) {
+  if (!ctx || !ms) return FS_ERR_ARG;
+  if (!ctx->kernel_timed) return fs_fail(ctx, FS_ERR_STATE, "no timed render (option \"time\")");
+  cudaSetDevice(ctx->device);
+  int e = cudaEventSynchronize(ctx->ev_kernel[1]);
+  if (!e) e = cudaEventElapsedTime(ms, ctx->ev_kernel[0], ctx->ev_kernel[1]);
+  if (e) return fs_cuda_fail(ctx, e, "kernel timer");
+  return FS_OK;
+}
+
+int fs_measure_l2_read_gbs(fs_ctx *ctx, int64_t bytes, int32_t reps, float *gbs) {
+  if (!ctx || !gbs || bytes < (1 << 20) || reps < 1) return FS_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  bytes &= ~(int64_t)15;
+  void *buf = NULL;
+  uint32_t *sink = NULL;
+  cudaEvent_t a = NULL, b = NULL;
+  int rc = FS_OK;
+  if (cudaMalloc(&buf, (size_t)bytes) || cudaMalloc((void **)&sink, 4)) {
+    rc = fs_fail(ctx, FS_ERR_NOMEM, "cudaMalloc(L2 probe)");
+    goto done;
+  }
+  if (cudaEventCreate(&a) || cudaEventCreate(&b)) {
+    rc = fs_fail(ctx, FS_ERR_CUDA, "cudaEventCreate(L2 probe)");
+    goto done;
+  }
+  {
+    const int32_t grid = 4 * ctx->sm_count;
+    int e = cudaMemsetAsync(buf, 1, (size_t)bytes, ctx->stream);
+    if (!e) e = fsk_l2_read(buf, bytes, 1, grid, sink, ctx->stream); /* into L2 */
+    if (!e) e = cudaEventRecord(a, ctx->stream);
+    if (!e) e = fsk_l2_read(buf, bytes, reps, grid, sink, ctx->stream);
+    if (!e) e = cudaEventRecord(b, ctx->stream);
+    if (!e) e = cudaEventSynchronize(b);
+    float ms = 0.0f;
+    if (!e) e = cudaEventElapsedTime(&ms, a, b);
+    if (e) {
+      rc = fs_cuda_fail(ctx, e, "L2 probe");
+      goto done;
+    }
+    *gbs = (float)((double)bytes * reps / (ms * 1e-3) / 1e9);
+  }
+done:
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  cudaFree(sink);
+  cudaFree(buf);
+  return rc;
 }
 
 int fs_ctx_stats(fs_ctx *ctx, int32_t enable, uint64_t out2[2]) {
@@ -607,6 +667,7 @@ int fs_render_view(fs_ctx *ctx, const FsMapDev *map, FsView *v, const FsTune *tu
   L->stride_max = stride;
   int e = fsk_ztable(NULL, &L->view0, 1, v->n, zline, zinvz, ctx->stream);
   if (e) return fs_cuda_fail(ctx, e, "z-table kernel launch");
+  if (ctx->time_kernel) cudaEventRecord(ctx->ev_kernel[0], ctx->stream);
   if (v->nseg > 1) {
     /* minimum row of every segment but the last, before the render pass */
     FsLaunch A = *L;
@@ -623,6 +684,10 @@ int fs_render_view(fs_ctx *ctx, const FsMapDev *map, FsView *v, const FsTune *tu
     e = fsk_gapfill(NULL, &L->view0, 1, v->W, ctx->stream);
     if (e) return fs_cuda_fail(ctx, e, "gap-fill kernel launch");
     ctx->launches++;
+  }
+  if (ctx->time_kernel) {
+    cudaEventRecord(ctx->ev_kernel[1], ctx->stream);
+    ctx->kernel_timed = 1;
   }
   return FS_OK;
 }

@@ -107,7 +107,8 @@ typedef struct {
   int32_t tw;    /* column-tile width: columns per CTA */
   int32_t lc;    /* lanes per column (32: one warp per column) */
   int32_t u;     /* depth samples per lane per chunk: chunk = lc * u depths */
-  int32_t stage; /* 1: shared-memory column stage + TMA store; 0: direct painting */
+  int32_t stage; /* 0: direct painting; 1: shared-memory column stage + TMA store;
+                  * 2: cooperative tile (lc = threads per column) */
   int32_t ctas;  /* persistent CTAs (0: as many as fit) */
   int32_t smooth; /* 1: the `#on` smoothing kernels (FS_TUNE_LIST_SM) */
   int32_t fx;     /* 1: kernels with the shading / fog epilogue compiled in */
@@ -130,6 +131,8 @@ int fsk_segmin(const FsLaunch *L, const FsTune *t, int32_t hf, int32_t grid, cud
 int fsk_gapfill(const FsView *views_dev, const FsView *view0, int32_t nviews, int32_t max_w,
                 cudaStream_t st);
 int32_t fsk_items_per_cta(const FsTune *t);
+int fsk_l2_read(const void *buf, int64_t bytes, int32_t reps, int32_t grid, uint32_t *sink,
+                cudaStream_t st);
 /* A work item names a view (or serving session), a depth segment and a column
  * tile (shared-memory stage) or strip (direct painting). */
 #define FS_ITEM_VIEWS 32768

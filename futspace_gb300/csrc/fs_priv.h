@@ -40,6 +40,9 @@ struct fs_ctx {
   unsigned long long *stats_dev;
   int32_t collect_stats;
   int64_t launches;
+  int32_t time_kernel;   /* 1: events around the render kernels of each plain call */
+  int32_t kernel_timed;  /* the events hold a completed call's timing */
+  cudaEvent_t ev_kernel[2];
   FsTune forced; /* tw == 0: choose per frame */
   int32_t ntune;
   fs_tune_entry tunes[FS_TUNE_CACHE_MAX];

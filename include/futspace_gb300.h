@@ -126,8 +126,14 @@ int fs_ctx_force_tune(fs_ctx *ctx, const int32_t tune5[5]);
  * too few column strips to occupy the GPU, split each column's depth range
  * into segments marched by separate warps, after a pass that finds each
  * segment's minimum row; 0: never). Plans capture the options at creation or
- * retuning. Pixels are identical either way. */
+ * retuning. Pixels are identical either way. Option "time" (0, default; 1:
+ * record CUDA events around the render kernels of every plain per-frame call,
+ * read with fs_ctx_kernel_ms) changes no pixel either. */
 int fs_ctx_set_option(fs_ctx *ctx, const char *name, int64_t value);
+/* Device time in ms of the render kernels (depth-table kernel excluded) of the
+ * last plain per-frame call made with option "time" on; waits for that call.
+ * FS_ERR_STATE when no such call was made. */
+int fs_ctx_kernel_ms(fs_ctx *ctx, float *ms);
 
 /* Page-locked host memory (cudaMallocHost) for frame downloads that should not
  * block the calling thread, e.g. fs_request.host_out. */
@@ -237,6 +243,13 @@ int fs_tune_get(int i, int32_t out5[5]);
  * the depth samples it evaluated and the occlusion events it coloured. Reading
  * (out2 != NULL) waits for the stream and resets the counters. */
 int fs_ctx_stats(fs_ctx *ctx, int32_t enable, uint64_t out2[2]);
+
+/* Roofline denominator: L2 read bandwidth in GB/s, from one kernel reading a
+ * `bytes`-long device buffer (at least 1 MiB, small enough to stay in L2)
+ * `reps` times with L2-only loads after a pass that brings it into L2; CUDA
+ * events on the context stream around the timed launch. Allocates and frees
+ * the buffer. */
+int fs_measure_l2_read_gbs(fs_ctx *ctx, int64_t bytes, int32_t reps, float *gbs);
 
 /* ---- serving: continuous batching of render requests -----------------------
  * A server keeps the maps and one view record per session resident on the

@@ -413,3 +413,29 @@ def test_cooperative_tile_1080p_frame(fs, orc, gpu_ctx):
         plan.run()
         bad = [i for i, (f, r) in enumerate(zip(plan.frames(), refs)) if count_diff(f, r)]
         assert not bad, (tune, bad)
+
+
+def test_plain_call_kernel_timer(fs, gpu_ctx, maps256):
+    """Option "time": events around the render kernels of a plain call; no pixel
+    changes, and reading the timer before any timed call is a state error."""
+    hm, cm = maps256
+    fmap = fs.Map(gpu_ctx, hm, cm)
+    cam = fs.gen_cameras(171, hm, 1, above=(30, 30), distance=(500, 500), screen_h=96)[0]
+    ref = gpu_ctx.render(fmap, cam, 128, 96)
+    with pytest.raises(fs.FsError) as ei:
+        gpu_ctx.kernel_ms()
+    assert ei.value.code == 6
+    gpu_ctx.set_option("time", 1)
+    try:
+        got = gpu_ctx.render(fmap, cam, 128, 96)
+        ms = gpu_ctx.kernel_ms()
+    finally:
+        gpu_ctx.set_option("time", 0)
+    assert count_diff(got, ref) == 0
+    assert 0.0 < ms < 1000.0
+
+
+def test_l2_read_probe(gpu_ctx):
+    """The roofline's L2 read bandwidth probe returns a finite positive rate."""
+    gbs = gpu_ctx.measure_l2_read_gbs(16 << 20, 8)
+    assert 100.0 < gbs < 1.0e6
