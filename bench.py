@@ -10,6 +10,12 @@ scale=w/2), bilinear height and colour. One step renders every view once with
 the persistent kernel replayed from a CUDA graph. The plain per-frame loop
 (two launches per view) is timed on the same plan for comparison.
 
+Workload "single1080": one 1920x1080 frame per step through the plain
+per-frame call (fs_render_device), the walk's cameras in turn, with the
+render-kernel time and the frame's gather/store roofline (frame bytes at the
+HBM copy peak vs the ncu-counted gather sectors at the live-measured L2 read
+rate).
+
 Prints one JSON line (rank 0). `value` is whole-job Gpix/s with maps resident
 in HBM; `e2e` is the same metric through the public C ABI with host buffers:
 per step the cameras go host->device and every frame device->pinned host.

@@ -2,7 +2,9 @@
  * Autotuner for the render kernel's knobs -- column-tile width (TW), lanes per
  * column (LC: 32 = one warp per column, 16/8/4 = two/four/eight columns per
  * warp), depth samples per lane per chunk (U: chunk = LC*U depths) and the
- * painting form (shared-memory stage + TMA store, or direct) -- plus its cache. Each candidate that fits in shared memory is timed with CUDA
+ * form (direct painting, shared-memory stage + TMA store, or the cooperative
+ * tile with LC threads per column and U depths per thread per block) -- plus
+ * its cache. Each candidate that fits in shared memory is timed with CUDA
  * events on the context stream; the fastest is stored under a key made of the
  * screen resolution (or a batch's resolution multiset), the map size and the
  * filters. The cache is a text file, one "key tw lc u stage" line per entry, read at
