@@ -221,6 +221,22 @@ def cpu_reference_rate(views, hm, cm, max_seconds: float, threads: int, params=N
     return px / dt / 1e9, used, px, dt
 
 
+def cpu_baselines(views, hm, cm, seconds: float, params=None, what: str = "views"):
+    """The oracle on the host cores: OpenMP over columns on every core (the
+    stand-in for a `futhark multicore` build) and one thread (for `futhark c`),
+    each on a bounded prefix of the workload's views."""
+    import oracle
+    threads = oracle.lib().fso_max_threads()
+    out = {}
+    for key, nt, budget in (("multi", threads, seconds), ("single", 1, seconds / 2)):
+        g, used, cpx, dt = cpu_reference_rate(views, hm, cm, budget, nt, params)
+        out[key] = {"value": g, "unit": "Gpix/s", "cores": nt, "kind": "port",
+                    "sample": f"first {used} {what} of the workload ({cpx} px, {dt:.1f} s), CPU "
+                              "oracle (C restatement of the reference render"
+                              + (", OpenMP over columns)" if nt > 1 else ", one thread)")}
+    return out["multi"], out["single"]
+
+
 def run_reference(args, rank: int, world: int):
     if rank != 0:
         return
@@ -444,15 +460,14 @@ def run_single(args, rank: int, world: int, local: int):
     store_us = 4 * W * H / (peaks["hbm_gbs"] * 1e3)
     gather_us = gather_bytes / (l2_gbs * 1e3)
     bound_us = max(store_us, gather_us)
+    # the same with the reference's full gather work, every depth sample of
+    # every column at 20 B (a 4-byte height quad, four colour texels): larger
+    # than what this kernel reads, which skips samples
+    full_us = max(store_us, n * W * 20 / (l2_gbs * 1e3))
 
-    cpu = None
+    cpu = cpu1 = None
     if rank == 0 and args.cpu_seconds > 0:
-        import oracle
-        threads = oracle.lib().fso_max_threads()
-        g, used, cpx, dt = cpu_reference_rate(views, hm, cm, args.cpu_seconds, threads)
-        cpu = {"value": g, "unit": "Gpix/s", "cores": threads, "kind": "port",
-               "sample": f"first {used} frames of the walk ({cpx} px, {dt:.1f} s), CPU oracle "
-                         "(C restatement of the reference render, OpenMP over columns)"}
+        cpu, cpu1 = cpu_baselines(views, hm, cm, args.cpu_seconds, what="frames")
     if rank == 0:
         line = {
             "metric": METRIC_SINGLE,
@@ -481,11 +496,14 @@ def run_single(args, rank: int, world: int, local: int):
                                       if sectors else "algorithmic gather bytes",
                                       "l2_read_gbs_measured": l2_gbs, "bound_us": bound_us,
                                       "kernel_us": k_ms * 1e3,
-                                      "frac": bound_us / (k_ms * 1e3)},
+                                      "frac": bound_us / (k_ms * 1e3),
+                                      "bound_us_full_work": full_us,
+                                      "frac_full_work": full_us / (k_ms * 1e3)},
             "clocks": clk,
             "e2e": e2e,
             "gpu_launches": gpu_launches,
             "cpu_baseline": cpu,
+            "cpu_baseline_one_thread": cpu1,
         }
         print(json.dumps(line), flush=True)
     if dist:
@@ -648,15 +666,10 @@ def main():
     achieved = alg / (k_ms * 1e-3) / 1e9
     traffic = profiled_traffic(args.workload)
 
-    cpu = None
+    cpu = cpu1 = None
     if rank == 0 and args.cpu_seconds > 0:
         import oracle
-        threads = oracle.lib().fso_max_threads()
-        g, used, cpx, dt = cpu_reference_rate(views, hm, cm, args.cpu_seconds, threads,
-                                              oracle.params_from(wparams))
-        cpu = {"value": g, "unit": "Gpix/s", "cores": threads, "kind": "port",
-               "sample": f"first {used} views of the workload ({cpx} px, {dt:.1f} s), CPU oracle "
-                         "(C restatement of the reference render, OpenMP over columns)"}
+        cpu, cpu1 = cpu_baselines(views, hm, cm, args.cpu_seconds, oracle.params_from(wparams))
 
     if rank == 0:
         full_s = sum(fs.num_depths(v[0].distance) * v[1] for v in views)
@@ -691,6 +704,7 @@ def main():
             "e2e": e2e,
             "gpu_launches": gpu_launches,
             "cpu_baseline": cpu,
+            "cpu_baseline_one_thread": cpu1,
         }
         if tune_info:
             line["config"]["autotune_ms"] = tune_info[1]
