@@ -999,37 +999,45 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
 
       /* Y: the minimum before each sample, the block's events (B), and the
        * next block's depth-table entries */
-      int prev = mstart;
-      for (int w = 0; w < warp; w++) prev = min(prev, wtot[w * TW + c]);
-      if (lane >= TW) prev = min(prev, ex);
-      if (j == TPC - 1) mcol[(par ^ 1) * TW + c] = min(prev, run);
-      int cnt = 0;
-      {
-        int pv = prev;
+      /* a run whose rows are all at or below the column's minimum at the
+       * block start holds no event; a warp of such runs skips the prefix,
+       * except the last warp, which records the columns' new minima */
+      if (warp == NW - 1 || __any_sync(FS_FULL_MASK, run < mstart)) {
+        int prev = mstart;
+        for (int w = 0; w < warp; w++) prev = min(prev, wtot[w * TW + c]);
+        if (lane >= TW) prev = min(prev, ex);
+        if (j == TPC - 1) mcol[(par ^ 1) * TW + c] = min(prev, run);
+        int cnt = 0;
+        if (run < prev) {
+          int pv = prev;
 #pragma unroll
-        for (int i = 0; i < U; i++)
-          if (r[i] < pv) {
-            cnt++;
-            pv = r[i];
+          for (int i = 0; i < U; i++)
+            if (r[i] < pv) {
+              cnt++;
+              pv = r[i];
+            }
+        }
+        int csum = cnt;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          const int t = __shfl_up_sync(FS_FULL_MASK, csum, off);
+          if (lane >= off) csum += t;
+        }
+        const int total = __shfl_sync(FS_FULL_MASK, csum, 31);
+        if (total) {
+          int base = 0;
+          if (lane == 31) base = atomicAdd(&scal[par], total);
+          base = __shfl_sync(FS_FULL_MASK, base, 31) + csum - cnt;
+          if (cnt) {
+            uint32_t *q = evq + par * ECAP;
+#pragma unroll
+            for (int i = 0; i < U; i++)
+              if (r[i] < prev) {
+                q[base++] = pack_coop_event(j * U + i, c, r[i]);
+                prev = r[i];
+              }
           }
-      }
-      int csum = cnt;
-#pragma unroll
-      for (int off = 1; off < 32; off <<= 1) {
-        const int t = __shfl_up_sync(FS_FULL_MASK, csum, off);
-        if (lane >= off) csum += t;
-      }
-      int base = 0;
-      if (lane == 31 && csum) base = atomicAdd(&scal[par], csum);
-      base = __shfl_sync(FS_FULL_MASK, base, 31) + csum - cnt;
-      if (cnt) {
-        uint32_t *q = evq + par * ECAP;
-#pragma unroll
-        for (int i = 0; i < U; i++)
-          if (r[i] < prev) {
-            q[base++] = pack_coop_event(j * U + i, c, r[i]);
-            prev = r[i];
-          }
+        }
       }
       const bool more = kb + NB < n;
       if (more) load_table(kb + NB, par ^ 1);
