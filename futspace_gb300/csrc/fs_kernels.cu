@@ -186,12 +186,17 @@ extern "C" int fsk_tune_supported(const FsTune *t) {
 #define FS_CASE_C(TW_, TPC_, U_)                                                      \
   if (t->stage == 2 && t->tw == TW_ && t->lc == TPC_ && t->u == U_ && !t->smooth && !t->fx) \
     return 1;
+#define FS_CASE_CF(TW_, TPC_, U_)                                                    \
+  if (t->stage == 2 && t->tw == TW_ && t->lc == TPC_ && t->u == U_ && !t->smooth && t->fx) \
+    return 1;
   FS_TUNE_LIST(FS_CASE)
   FS_TUNE_LIST_MODES(FS_CASE_M)
   FS_COOP_LIST(FS_CASE_C)
+  FS_COOP_LIST_FX(FS_CASE_CF)
 #undef FS_CASE
 #undef FS_CASE_M
 #undef FS_CASE_C
+#undef FS_CASE_CF
   return 0;
 }
 

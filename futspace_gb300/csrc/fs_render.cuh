@@ -38,6 +38,9 @@
  *           footprint, full occupancy); the warp then writes its columns' sky
  *           rows, a row per store instruction, and re-runs the gap fill over a
  *           column that painted the gap colour.
+ * A third kernel, the cooperative tile (coop_kernel, tuning stage 2, at the
+ * end of this file), marches all depths of a column tile at once for frames
+ * with too few columns to keep the GPU busy.
  */
 #pragma once
 #include "fs_device.cuh"
@@ -859,7 +862,7 @@ __device__ __forceinline__ uint32_t pack_coop_event(int kl, int c, int row) {
   return ((uint32_t)kl << 21) | ((uint32_t)c << 16) | (uint32_t)row;
 }
 
-template <int TW, int TPC, int U, int HF, int CF>
+template <int TW, int TPC, int U, int HF, int CF, int FX>
 __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
     coop_kernel(const __grid_constant__ FsLaunch P) {
   using S = CoopShape<TW, TPC, U>;
@@ -923,7 +926,8 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
       }
     };
     /* colour the events of the block in buffer half, each at its row */
-    auto colour_events = [&](int half) {
+    /* (kbc: the first depth of that block, for the optional epilogue) */
+    auto colour_events = [&](int half, int kbc) {
       const int ne = scal[half];
       if (P.stats && tid == 0) n_events += (uint32_t)ne;
       for (int e = tid; e < ne; e += NT) {
@@ -932,8 +936,16 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
         const float4 L = zt[half * NB + (kl % U) * TPC + kl / U];
         const float2 xy =
             axpy2((float)(c0 + ec), make_float2(L.z, L.w), make_float2(L.x, L.y));
-        stage[er * TW + ec] =
-            CF ? color_bilinear(M, chan, xy.x, xy.y) : color_nearest(M, xy.x, xy.y);
+        uint32_t colour = CF ? color_bilinear(M, chan, xy.x, xy.y) : color_nearest(M, xy.x, xy.y);
+        if constexpr (FX) {
+          if (Vp->flags & (FSV_SHADE | FSV_FOG)) {
+            /* depth of sample k, as the depth table computes it */
+            const float fi = (float)(kbc + kl + 1);
+            const float z = fm(fd(fi, 2.0f), fa(fm(2.0f, Vp->z0), fm(fs(fi, 1.0f), Vp->d)));
+            colour = apply_effects(chan, *Vp, colour, z);
+          }
+        }
+        stage[er * TW + ec] = colour;
       }
     };
 
@@ -983,7 +995,7 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
           rows(BoolTag<false>{});
         if (P.stats) n_samples += (uint32_t)max(0, min(U, n - kb - j * U));
       }
-      if (kb > 0) colour_events(par ^ 1);
+      if (kb > 0) colour_events(par ^ 1, kb - NB);
       int run = H;
 #pragma unroll
       for (int i = 0; i < U; i++) run = min(run, r[i]);
@@ -1053,7 +1065,7 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
         done = all0;
       }
       if (done) {
-        colour_events(par);
+        colour_events(par, kb);
         fin = par ^ 1;
         break;
       }
@@ -1090,6 +1102,11 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
   X(4, 64, 8)           \
   X(8, 32, 8)           \
   X(4, 64, 4)
+
+/* Cooperative tile configurations with the shading / fog epilogue. */
+#define FS_COOP_LIST_FX(X) \
+  X(8, 64, 8)              \
+  X(4, 64, 8)
 
 /* Kernel modes beyond the plain render, each compiled for a few configurations
  * and every filter pair: (TW, LC, U, STG, smoothing, epilogue). The epilogue

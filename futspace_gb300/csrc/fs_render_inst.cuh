@@ -1,6 +1,7 @@
 /*
  * Instantiates the render kernels for one (height filter, colour filter) pair:
- * every configuration of FS_TUNE_LIST, FS_TUNE_LIST_MODES and FS_COOP_LIST. Included by fs_render_h?c?.cu with
+ * every configuration of FS_TUNE_LIST, FS_TUNE_LIST_MODES, FS_COOP_LIST and
+ * FS_COOP_LIST_FX. Included by fs_render_h?c?.cu with
  * FS_HF, FS_CF and FS_RENDER_ENTRY defined, so the four pairs compile as
  * separate translation units in parallel.
  *
@@ -39,11 +40,15 @@ extern "C" int FS_RENDER_ENTRY(int op, const FsLaunch *L, const FsTune *t, int g
 #undef FS_CASE
 #undef FS_CASE_M
 #undef FS_CASE_S
-/* the cooperative tile form (plain mode only) */
-#define FS_COOP_CASE(TW_, TPC_, U_)                                                          \
-  if (t->stage == 2 && t->tw == TW_ && t->lc == TPC_ && t->u == U_ && !t->smooth && !t->fx) { \
+/* the cooperative tile form (plain mode; a few configurations with the
+ * epilogue) */
+#define FS_COOP_CASE(TW_, TPC_, U_) FS_COOP_CASE_F(TW_, TPC_, U_, 0)
+#define FS_COOP_CASE_FX(TW_, TPC_, U_) FS_COOP_CASE_F(TW_, TPC_, U_, 1)
+#define FS_COOP_CASE_F(TW_, TPC_, U_, FX_)                                                   \
+  if (t->stage == 2 && t->tw == TW_ && t->lc == TPC_ && t->u == U_ && !t->smooth &&         \
+      t->fx == FX_) {                                                                      \
     static int smem_set[64];                                                               \
-    auto kern = fsd::coop_kernel<TW_, TPC_, U_, FS_HF, FS_CF>;                             \
+    auto kern = fsd::coop_kernel<TW_, TPC_, U_, FS_HF, FS_CF, FX_>;                        \
     if (smem_set[dev] < (int)smem) {                                                       \
       e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
       if (e != cudaSuccess) return (int)e;                                                 \
@@ -55,7 +60,10 @@ extern "C" int FS_RENDER_ENTRY(int op, const FsLaunch *L, const FsTune *t, int g
     return (int)cudaGetLastError();                                                        \
   }
   FS_COOP_LIST(FS_COOP_CASE)
+  FS_COOP_LIST_FX(FS_COOP_CASE_FX)
 #undef FS_COOP_CASE
+#undef FS_COOP_CASE_FX
+#undef FS_COOP_CASE_F
   return (int)cudaErrorInvalidValue;
 }
 
