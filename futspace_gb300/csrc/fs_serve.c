@@ -119,9 +119,12 @@ struct fs_server {
   FsMapDev maps[FS_MAX_MAPS];
   fs_params params;
   fs_server_config cfg;
-  FsTune tune;
+  FsTune tune;      /* direct painting */
+  FsTune tune_coop; /* the cooperative tile, when use_coop */
+  int32_t use_coop;
   int32_t hf, cf, grid, max_items;
-  int32_t iw; /* screen columns per work item */
+  int32_t iw;      /* screen columns per work item, direct painting */
+  int32_t iw_coop; /* and the cooperative tile */
   uint8_t *arena_base;
   fs_arena arena;
   FsView *sess_d;
@@ -203,10 +206,21 @@ int fs_server_new(fs_ctx *ctx, fs_server **out, const fs_map *const *maps, int32
   }
   s->hf = params->height_filter == FS_BILINEAR;
   s->cf = params->color_filter == FS_BILINEAR;
-  /* serving paints frames directly (no shared-memory stage, no tensor maps) */
+  /* Two forms, chosen per launch: the cooperative tile (CTA tiles, frames
+   * stored from shared memory with plain stores, no tensor maps) for every
+   * launch whose tallest frame fits its stage, else direct painting. Serving
+   * batches are small, and few strips leave direct painting latency-bound. An
+   * explicit tuning names one form: stage 0 direct only; stage 2 the
+   * cooperative tile, with direct painting for frames too tall for it. */
   FsTune t = {cfg->tune[0], cfg->tune[1], cfg->tune[2], cfg->tune[3], cfg->tune[4]};
+  FsTune c = {0, 0, 0, 0, 0};
+  const FsTune def = {128, 1, 4, 0, 0};
+  const FsTune def_coop = {8, 64, 8, 2, 0};
   if (!t.tw) {
-    FsTune def = {128, 1, 4, 0, 0};
+    t = def;
+    c = def_coop;
+  } else if (t.stage == 2) {
+    c = t;
     t = def;
   }
   {
@@ -215,20 +229,32 @@ int fs_server_new(fs_ctx *ctx, fs_server **out, const fs_map *const *maps, int32
     const int32_t flags = (params->smoothing ? FSV_SMOOTH : 0) |
                           ((params->effects & FS_FX_SHADE) ? FSV_SHADE : 0) |
                           ((params->effects & FS_FX_FOG) ? FSV_FOG : 0);
-    if (cfg->tune[0]) {
+    if (cfg->tune[0] && cfg->tune[3] == 0) {
       t.smooth = (flags & FSV_SMOOTH) ? 1 : 0;
       t.fx = (flags & (FSV_SHADE | FSV_FOG)) ? 1 : 0;
     } else {
       t = fs_tune_for_mode(t, flags);
     }
+    c.smooth = (flags & FSV_SMOOTH) ? 1 : 0;
+    c.fx = (flags & (FSV_SHADE | FSV_FOG)) ? 1 : 0;
   }
   if (t.stage != 0 || !fsk_tune_supported(&t)) {
     fs_server_free(s);
     return fs_fail(ctx, FS_ERR_ARG, "serving needs a compiled direct-paint configuration");
   }
+  s->use_coop = c.tw && fsk_tune_supported(&c);
+  if (cfg->tune[0] && cfg->tune[3] == 2 && !s->use_coop) {
+    fs_server_free(s);
+    return fs_fail(ctx, FS_ERR_ARG, "no cooperative tile compiled for this mode");
+  }
   s->tune = t;
   s->iw = fsk_item_width(&t);
-  s->max_items = cfg->max_batch * ((65536 + s->iw - 1) / s->iw);
+  s->tune_coop = c;
+  s->iw_coop = s->use_coop ? fsk_item_width(&c) : s->iw;
+  {
+    const int32_t iw_min = s->iw < s->iw_coop ? s->iw : s->iw_coop;
+    s->max_items = cfg->max_batch * ((65536 + iw_min - 1) / iw_min);
+  }
   int32_t occ = 0;
   int e = fsk_render_max_ctas_per_sm(&t, s->hf, s->cf, 1, &occ);
   if (e || occ < 1) {
@@ -299,12 +325,13 @@ static int launch_batch(fs_server *s, fs_slot *sl, fs_request *reqs, fs_fifo *re
   FsView *packed = (FsView *)sl->pinned;
   int32_t *ids = (int32_t *)(sl->pinned + sizeof(FsView) * (size_t)mb);
   int64_t *items = (int64_t *)(sl->pinned + items_offset(s));
-  int32_t nb = 0, ni = 0;
+  int32_t nb = 0, ni = 0, hmax = 0;
+  const int32_t iw_min = s->iw < s->iw_coop ? s->iw : s->iw_coop;
   sl->nreq = 0;
   while (ready->head < ready->tail && nb < mb) {
     const int32_t ri = ready->q[ready->head % ready->cap];
     fs_request *r = &reqs[ri];
-    const int32_t tiles = (r->width + s->iw - 1) / s->iw;
+    const int32_t tiles = (r->width + iw_min - 1) / iw_min;
     if (ni + tiles > s->max_items) break;
     ready->head++;
     FsView v;
@@ -326,17 +353,36 @@ static int launch_batch(fs_server *s, fs_slot *sl, fs_request *reqs, fs_fifo *re
     v.tmap = -1;
     packed[nb] = v;
     ids[nb] = r->session;
-    for (int32_t t = 0; t < tiles; t++) {
-      scratch[ni].cost = (int64_t)v.n * 8 + v.H;
-      scratch[ni].item = FS_ITEM(r->session, 0, t);
-      ni++;
-    }
+    ni += tiles; /* capacity at the narrower item width */
+    if (v.H > hmax) hmax = v.H;
     sl->req[nb] = ri;
     r->batch = batch_id;
     r->start_ns = now_ns() - t0;
     nb++;
   }
   if (nb == 0) return FS_OK;
+  /* the form of this launch: the cooperative tile if the tallest frame's
+   * stage fits in shared memory */
+  const FsTune *tune = &s->tune;
+  int32_t iw = s->iw, grid_max = s->grid, stride = 1;
+  if (s->use_coop && fsk_render_smem(&s->tune_coop, hmax | 1) <= ctx->smem_optin) {
+    int32_t occ = 0;
+    if (!fsk_render_max_ctas_per_sm(&s->tune_coop, s->hf, s->cf, hmax | 1, &occ) && occ > 0) {
+      tune = &s->tune_coop;
+      iw = s->iw_coop;
+      grid_max = occ * ctx->sm_count;
+      stride = hmax | 1;
+    }
+  }
+  ni = 0;
+  for (int32_t b = 0; b < nb; b++) {
+    const int32_t tiles = (packed[b].W + iw - 1) / iw;
+    for (int32_t t = 0; t < tiles; t++) {
+      scratch[ni].cost = (int64_t)packed[b].n * 8 + packed[b].H;
+      scratch[ni].item = FS_ITEM(ids[b], 0, t);
+      ni++;
+    }
+  }
   qsort(scratch, (size_t)ni, sizeof(srv_item), cmp_item);
   for (int32_t i = 0; i < ni; i++) items[i] = scratch[i].item;
   sl->nreq = nb;
@@ -361,11 +407,11 @@ static int launch_batch(fs_server *s, fs_slot *sl, fs_request *reqs, fs_fifo *re
     L.head = sl->head_d;
     L.stats = ctx->stats_dev;
     L.nitems = ni;
-    L.stride_max = 1;
-    const int32_t per_cta = fsk_items_per_cta(&s->tune);
+    L.stride_max = stride;
+    const int32_t per_cta = fsk_items_per_cta(tune);
     const int32_t need = (ni + per_cta - 1) / per_cta;
-    const int32_t grid = need < s->grid ? need : s->grid;
-    e = fsk_render(&L, &s->tune, s->hf, s->cf, grid, sl->st);
+    const int32_t grid = need < grid_max ? need : grid_max;
+    e = fsk_render(&L, tune, s->hf, s->cf, grid, sl->st);
     ctx->launches += 2;
   }
   for (int32_t i = 0; i < nb && !e; i++) {

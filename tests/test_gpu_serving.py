@@ -35,13 +35,17 @@ def _fill(fs, specs, bufs, arrivals=None):
     return arr
 
 
-def test_alone_equals_mix_equals_oracle(fs, orc, gpu_ctx, maps1024, maps256):
+@pytest.mark.parametrize("tune", [None, (128, 1, 4, 0), (8, 64, 8, 2)],
+                         ids=["default", "direct", "cooperative"])
+def test_alone_equals_mix_equals_oracle(fs, orc, gpu_ctx, maps1024, maps256, tune):
+    """The default server (cooperative tile per launch where the tallest frame
+    fits, else direct painting) and each form alone."""
     maps_np = [maps1024, maps256]
     fmaps = [fs.Map(gpu_ctx, h, c) for h, c in maps_np]
     specs = _requests(fs, maps_np, nsess=8, per_sess=4, seed=5)
     bufs = [fs.PinnedBuffer((h, w)) for (_, _, w, h, _) in specs]
     srv = fs.Server(gpu_ctx, fmaps, budget_bytes=16 << 20, nsessions=8, max_batch=8, slots=3,
-                    max_distance=1200.0)
+                    max_distance=1200.0, tune=tune)
     try:
         # in the mix: everything released at once (admission + batching decide)
         reqs = _fill(fs, specs, bufs)
