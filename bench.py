@@ -324,6 +324,14 @@ def run_serve(args, rank: int, world: int):
                 bufs[i] = fs.PinnedBuffer((h, w))
                 r.host_out = bufs[i].ptr
         st = srv.run(reqs, realtime=True)
+        # where the slowest requests arrived (a stall shows as one window)
+        lat = np.array([(reqs[i].done_ns - reqs[i].arrival_ns) * 1e-6 for i in range(n)])
+        arr_s = arrivals * 1e-9
+        late = lat > 10.0 * max(st["p50_ms"], 1e-3)
+        stall = {"max_ms": float(lat.max()) if n else 0.0,
+                 "late_requests": int(late.sum()),
+                 "late_arrivals_s": [float(arr_s[late].min()), float(arr_s[late].max())]
+                 if late.any() else None}
         p = fs.default_params()
         for i, b in bufs.items():
             r = reqs[i]
@@ -336,7 +344,7 @@ def run_serve(args, rank: int, world: int):
         results.append({"rate_req_s": rate, "requests": n, "offered_gpix_s": offered,
                         "gpix_s": st["gpix_s"], "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
                         "mean_batch": st["mean_batch"], "batches": st["batches"],
-                        "max_inflight": st["max_inflight"],
+                        "max_inflight": st["max_inflight"], "stall": stall,
                         "peak_arena_gb": st["peak_arena_bytes"] / 2**30, "errors": st["errors"]})
     srv.close()
     if rank == 0:

@@ -125,6 +125,9 @@ struct fs_server {
   int32_t hf, cf, grid, max_items;
   int32_t iw;      /* screen columns per work item, direct painting */
   int32_t iw_coop; /* and the cooperative tile */
+  /* cooperative-tile CTAs per SM by frame height in 32-row steps (0: not
+   * queried yet, -1: the stage does not fit) */
+  int16_t coop_occ[FS_MAX_ROWS / 32 + 2];
   uint8_t *arena_base;
   fs_arena arena;
   FsView *sess_d;
@@ -255,6 +258,15 @@ int fs_server_new(fs_ctx *ctx, fs_server **out, const fs_map *const *maps, int32
     const int32_t iw_min = s->iw < s->iw_coop ? s->iw : s->iw_coop;
     s->max_items = cfg->max_batch * ((65536 + iw_min - 1) / iw_min);
   }
+  if (s->use_coop) {
+    /* raise the kernel's shared-memory limit once, for the tallest frame
+     * whose stage fits, so no launch changes a function attribute */
+    int32_t rows = (FS_MAX_ROWS + 31) / 32 * 32;
+    while (rows > 32 && fsk_render_smem(&c, rows - 1) > ctx->smem_optin) rows -= 32;
+    int32_t occ = 0;
+    if (fsk_render_smem(&c, rows - 1) <= ctx->smem_optin)
+      fsk_render_max_ctas_per_sm(&c, s->hf, s->cf, rows - 1, &occ);
+  }
   int32_t occ = 0;
   int e = fsk_render_max_ctas_per_sm(&t, s->hf, s->cf, 1, &occ);
   if (e || occ < 1) {
@@ -365,13 +377,21 @@ static int launch_batch(fs_server *s, fs_slot *sl, fs_request *reqs, fs_fifo *re
    * stage fits in shared memory */
   const FsTune *tune = &s->tune;
   int32_t iw = s->iw, grid_max = s->grid, stride = 1;
-  if (s->use_coop && fsk_render_smem(&s->tune_coop, hmax | 1) <= ctx->smem_optin) {
-    int32_t occ = 0;
-    if (!fsk_render_max_ctas_per_sm(&s->tune_coop, s->hf, s->cf, hmax | 1, &occ) && occ > 0) {
+  if (s->use_coop) {
+    const int32_t cls = (hmax | 1) / 32; /* stages of one class round to the same rows */
+    if (!s->coop_occ[cls]) {
+      const int32_t st_rows = cls * 32 + 31; /* the class's tallest stride */
+      int32_t occ = 0;
+      if (fsk_render_smem(&s->tune_coop, st_rows) > ctx->smem_optin ||
+          fsk_render_max_ctas_per_sm(&s->tune_coop, s->hf, s->cf, st_rows, &occ) || occ < 1)
+        occ = -1;
+      s->coop_occ[cls] = (int16_t)occ;
+    }
+    if (s->coop_occ[cls] > 0) {
       tune = &s->tune_coop;
       iw = s->iw_coop;
-      grid_max = occ * ctx->sm_count;
-      stride = hmax | 1;
+      grid_max = s->coop_occ[cls] * ctx->sm_count;
+      stride = cls * 32 + 31;
     }
   }
   ni = 0;

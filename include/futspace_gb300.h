@@ -267,7 +267,11 @@ typedef struct {
   int32_t max_batch;    /* requests per launch */
   int32_t slots;        /* launches in flight */
   int32_t max_depths;   /* depth capacity per session (fs_num_depths of the largest distance) */
-  int32_t tune[5];      /* kernel configuration; tile width 0 = default */
+  int32_t tune[5];      /* kernel configuration {tw, lc, u, stage, ctas}; tile width 0 =
+                         * default: each launch uses the cooperative tile when its
+                         * tallest frame fits the tile's stage, else direct painting;
+                         * stage 0 = direct painting only; stage 2 = that cooperative
+                         * tile, direct painting for frames too tall for it */
 } fs_server_config;
 
 typedef struct {
