@@ -673,6 +673,15 @@ def main():
     k_ms = float(np.mean(t_kernel)) if t_kernel else ms
     achieved = alg / (k_ms * 1e-3) / 1e9
     traffic = profiled_traffic(args.workload)
+    # gather/store roofline of the launch: the slower of the frame bytes at the
+    # HBM copy peak and the gathers' L2 read sectors (committed ncu summary of
+    # this workload; else the algorithmic gather bytes) at the live L2 read rate
+    l2_gbs = max(ctx.measure_l2_read_gbs() for _ in range(3))
+    sectors = profiled_value(args.workload, "l2_read_sectors_per_launch")
+    gather_bytes = 32 * sectors if sectors else vb["height_gather"] + vb["color_gather"]
+    gs_store_ms = vb["frame"] / (peaks["hbm_gbs"] * 1e6)
+    gs_gather_ms = gather_bytes / (l2_gbs * 1e6)
+    gs_bound_ms = max(gs_store_ms, gs_gather_ms)
 
     cpu = cpu1 = None
     if rank == 0 and args.cpu_seconds > 0:
@@ -708,6 +717,12 @@ def main():
                          "traffic": traffic, "peak_source": peaks["source"],
                          "kernel": "render_kernel (persistent, one launch per step)",
                          "kernel_ms": k_ms, "bytes_per_launch": vb},
+            "gather_store_roofline": {"store_ms": gs_store_ms, "gather_ms": gs_gather_ms,
+                                      "gather_bytes": gather_bytes,
+                                      "gather_bytes_source": "ncu L2 read sectors x 32"
+                                      if sectors else "algorithmic gather bytes",
+                                      "l2_read_gbs_measured": l2_gbs, "bound_ms": gs_bound_ms,
+                                      "kernel_ms": k_ms, "frac": gs_bound_ms / k_ms},
             "clocks": clk,
             "e2e": e2e,
             "gpu_launches": gpu_launches,

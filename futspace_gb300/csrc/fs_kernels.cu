@@ -210,7 +210,8 @@ extern "C" size_t fsk_render_smem(const FsTune *t, int32_t stride_max) {
   const size_t nw = (size_t)t->tw * t->lc / 32;
   const size_t box = t->stage ? 2ull * kBoxRows * t->tw * 4 : 0;
   const size_t stage = t->stage ? (size_t)t->tw * stride_max * 4 : 0;
-  return box + nw * queue_cap(t->u) * 8 * (t->smooth ? 2 : 1) + 256 * 4 + stage;
+  return box + nw * queue_cap(t->u) * 8 * (t->smooth ? 2 : 1) + 256 * 4 + (t->stage ? 16 : 0) +
+         stage;
 }
 
 /* Screen columns per work item: a CTA tile with the shared-memory stage (and

@@ -145,7 +145,8 @@ struct RenderShape {
   static constexpr size_t box_bytes = STG ? 2ull * kBoxRows * TW * 4 : 0;
   static constexpr size_t queue_bytes = (size_t)NW * QCAP * 8 * QW;
   static constexpr size_t lut_bytes = 256 * 4;
-  static constexpr size_t fixed_bytes = box_bytes + queue_bytes + lut_bytes;
+  static constexpr size_t item_bytes = STG ? 16 : 0; /* the CTA's next item */
+  static constexpr size_t fixed_bytes = box_bytes + queue_bytes + lut_bytes + item_bytes;
   /* direct painting keeps 64 registers per thread so 32 warps fit per SM:
    * the march is bound by gather latency, and occupancy hides it */
   static constexpr int min_blocks = STG ? 1 : (NT >= 1024 ? 1 : 1024 / NT);
@@ -593,6 +594,7 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
   uint32_t *box = reinterpret_cast<uint32_t *>(smem);
   unsigned long long *queues = reinterpret_cast<unsigned long long *>(smem + S::box_bytes);
   float *lut = reinterpret_cast<float *>(smem + S::box_bytes + S::queue_bytes);
+  int *s_next = reinterpret_cast<int *>(smem + S::box_bytes + S::queue_bytes + S::lut_bytes);
   uint32_t *stage = reinterpret_cast<uint32_t *>(smem + S::fixed_bytes);
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -608,14 +610,13 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
   if constexpr (STG) {
     /* a CTA per (view, tile of TW columns): march into the column stage,
      * fill, then transpose and store with TMA (whole columns: one segment) */
-    __shared__ int s_item;
     const int cl = warp * CPW + lane / LC;
     for (int iter = 0;; iter++) {
       int item;
       if (P.head) {
-        if (tid == 0) s_item = atomicAdd(P.head, 1);
+        if (tid == 0) *s_next = atomicAdd(P.head, 1);
         __syncthreads();
-        item = s_item;
+        item = *s_next;
       } else {
         item = iter == 0 ? (int)blockIdx.x : P.nitems;
       }
