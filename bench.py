@@ -496,7 +496,9 @@ def run_single(args, rank: int, world: int, local: int):
                          "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
                          "traffic": profiled_traffic("single1080"),
                          "peak_source": peaks["source"],
-                         "kernel": "render kernel of one plain call", "kernel_ms": k_ms,
+                         "kernel": "the kernels of one plain call (depth table + render, "
+                                   "the render a programmatic dependent launch)",
+                         "kernel_ms": k_ms,
                          "bytes_per_launch": vb},
             "gather_store_roofline": {"store_us": store_us, "gather_us": gather_us,
                                       "gather_bytes": gather_bytes,

@@ -374,7 +374,7 @@ class Context:
         self.check(lib().fs_ctx_force_tune(self._h, t), "force_tune")
 
     def kernel_ms(self) -> float:
-        """Render-kernel device time of the last plain call made with option "time"."""
+        """Device time of the kernels of the last plain call made with option "time"."""
         ms = C.c_float()
         self.check(lib().fs_ctx_kernel_ms(self._h, C.byref(ms)), "kernel_ms")
         return ms.value

@@ -665,9 +665,11 @@ int fs_render_view(fs_ctx *ctx, const FsMapDev *map, FsView *v, const FsTune *tu
   L->stats = ctx->stats_dev;
   L->nitems = ntiles * v->nseg;
   L->stride_max = stride;
+  /* the timer brackets every kernel of the call; an event between two of them
+   * would stop the second from starting early */
+  if (ctx->time_kernel) cudaEventRecord(ctx->ev_kernel[0], ctx->stream);
   int e = fsk_ztable(NULL, &L->view0, 1, v->n, zline, zinvz, ctx->stream);
   if (e) return fs_cuda_fail(ctx, e, "z-table kernel launch");
-  if (ctx->time_kernel) cudaEventRecord(ctx->ev_kernel[0], ctx->stream);
   if (v->nseg > 1) {
     /* minimum row of every segment but the last, before the render pass */
     FsLaunch A = *L;
@@ -677,7 +679,9 @@ int fs_render_view(fs_ctx *ctx, const FsMapDev *map, FsView *v, const FsTune *tu
     if (e) return fs_cuda_fail(ctx, e, "segment-minimum kernel launch");
     ctx->launches++;
   }
-  e = fsk_render(L, &t, hf, cf, (L->nitems + per_cta - 1) / per_cta, ctx->stream);
+  /* programmatic dependent launch: the render kernel starts while the kernel
+   * before it finishes and waits for its results in the kernel */
+  e = fsk_render_pdl(L, &t, hf, cf, (L->nitems + per_cta - 1) / per_cta, ctx->stream);
   if (e) return fs_cuda_fail(ctx, e, "render kernel launch");
   ctx->launches += 2;
   if (v->nseg > 1) {

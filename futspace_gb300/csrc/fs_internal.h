@@ -120,6 +120,8 @@ int fsk_ztable(const FsView *views_dev, const FsView *view0, int32_t nviews, int
                float4 *zline, float *zinvz, cudaStream_t st);
 int fsk_render(const FsLaunch *L, const FsTune *t, int32_t hf, int32_t cf, int32_t grid,
                cudaStream_t st);
+int fsk_render_pdl(const FsLaunch *L, const FsTune *t, int32_t hf, int32_t cf, int32_t grid,
+                   cudaStream_t st);
 int fsk_serve_prepare(const FsView *packed_dev, const int32_t *ids_dev, int32_t nb, int32_t max_n,
                       FsView *sess_dev, float4 *zline, float *zinvz, cudaStream_t st);
 size_t fsk_render_smem(const FsTune *t, int32_t stride_max);

@@ -44,6 +44,7 @@ __device__ __forceinline__ void ztable_fill(const FsView *Vp, float4 *zline, flo
 }
 
 __global__ void ztable_kernel(const FsView *views, FsView view0, float4 *zline, float *zinvz) {
+  allow_dependent_launch();
   ztable_fill(views ? views + blockIdx.y : &view0, zline, zinvz);
 }
 
@@ -51,6 +52,7 @@ __global__ void ztable_kernel(const FsView *views, FsView view0, float4 *zline, 
  * table at ids[i], and its depth table is built. */
 __global__ void serve_prepare_kernel(const FsView *packed, const int32_t *ids, FsView *sess,
                                      float4 *zline, float *zinvz) {
+  allow_dependent_launch();
   const FsView *Vp = packed + blockIdx.y;
   if (blockIdx.x == 0 && threadIdx.x == 0) sess[ids[blockIdx.y]] = *Vp;
   ztable_fill(Vp, zline, zinvz);
@@ -286,6 +288,14 @@ extern "C" int fsk_render(const FsLaunch *L, const FsTune *t, int32_t hf, int32_
                           int32_t grid, cudaStream_t st) {
   if (grid <= 0) return (int)cudaSuccess;
   return pick(hf, cf)(0, L, t, grid, fsk_render_smem(t, L->stride_max), st, nullptr);
+}
+
+/* The same launch with programmatic stream serialization: it may start while
+ * the kernel before it on the stream runs, and waits for it in the kernel. */
+extern "C" int fsk_render_pdl(const FsLaunch *L, const FsTune *t, int32_t hf, int32_t cf,
+                              int32_t grid, cudaStream_t st) {
+  if (grid <= 0) return (int)cudaSuccess;
+  return pick(hf, cf)(2, L, t, grid, fsk_render_smem(t, L->stride_max), st, nullptr);
 }
 
 extern "C" int fsk_gapfill(const FsView *views_dev, const FsView *view0, int32_t nviews,

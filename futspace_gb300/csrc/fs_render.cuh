@@ -111,6 +111,19 @@ __device__ __forceinline__ void bulk_wait_all() {
   asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
 }
 
+/* Programmatic dependent launch: a render kernel launched with programmatic
+ * stream serialization may start while the kernel before it (the depth table,
+ * the serving prologue, the segment pass) still runs; it waits here, before
+ * its first read of anything that kernel writes. Without that launch
+ * attribute the wait returns at once. */
+__device__ __forceinline__ void wait_prior_grid() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+/* Lets the dependent grid launch before this one finishes. */
+__device__ __forceinline__ void allow_dependent_launch() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 /* fill_vline scan + sky (fut/voxel_renderer.fut:78-81, 246-248) over rows
  * [y_begin, H) of one column, one warp, 32 rows per step. `at(y)` addresses row
  * y. Rows above the column's final minimum row `mf` were never painted and
@@ -603,6 +616,7 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
   unsigned lanemask_lt;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lanemask_lt));
   for (int i = tid; i < 256; i += NT) lut[i] = __fdiv_rn((float)i, 255.0f);
+  wait_prior_grid();
   __syncthreads();
   const LutChannels chan{lut};
   uint32_t n_samples = 0, n_events = 0; /* work counters (ctx stats) */
@@ -732,6 +746,7 @@ __global__ void __launch_bounds__(TW *LC, 1024 / (TW * LC)) segmin_kernel(
   static_assert(CH <= FS_ZPAD, "a chunk reads at most FS_ZPAD depth-table entries past n");
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int dl = lane % LC, cl = lane / LC;
+  wait_prior_grid();
   for (int iter = 0;; iter++) {
     int item;
     if (P.head) {
@@ -886,6 +901,7 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
   const int c = tid % TW; /* the thread's column within the tile (lane % TW) */
   const int j = tid / TW; /* its run within each depth block */
   for (int i = tid; i < 256; i += NT) lut[i] = __fdiv_rn((float)i, 255.0f);
+  wait_prior_grid();
   const LutChannels chan{lut};
   uint32_t n_samples = 0, n_events = 0;
 

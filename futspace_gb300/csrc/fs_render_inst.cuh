@@ -5,9 +5,37 @@
  * FS_HF, FS_CF and FS_RENDER_ENTRY defined, so the four pairs compile as
  * separate translation units in parallel.
  *
- * op 0: launch `grid` CTAs; op 1: occupancy query (CTAs per SM) into *occ.
+ * op 0: launch `grid` CTAs; op 1: occupancy query (CTAs per SM) into *occ;
+ * op 2: launch with programmatic stream serialization.
  */
+#include <string.h>
+
 #include "fs_render.cuh"
+
+#ifndef FS_LAUNCH_HELPER
+#define FS_LAUNCH_HELPER
+/* op 0: a plain launch; op 2: with programmatic stream serialization */
+template <class K>
+static int fs_launch(int op, K kern, int grid, int block, size_t smem, cudaStream_t st,
+                     const FsLaunch *L) {
+  if (op == 2) {
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return (int)cudaLaunchKernelEx(&cfg, kern, *L);
+  }
+  kern<<<grid, block, smem, st>>>(*L);
+  return (int)cudaGetLastError();
+}
+#endif
 
 extern "C" int FS_RENDER_ENTRY(int op, const FsLaunch *L, const FsTune *t, int grid,
                                size_t smem, cudaStream_t st, int *occ) {
@@ -32,8 +60,7 @@ extern "C" int FS_RENDER_ENTRY(int op, const FsLaunch *L, const FsTune *t, int g
     }                                                                                      \
     if (op == 1) return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern,      \
                                                                            TW_ * LC_, smem); \
-    kern<<<grid, TW_ * LC_, smem, st>>>(*L);                                               \
-    return (int)cudaGetLastError();                                                        \
+    return fs_launch(op, kern, grid, TW_ * LC_, smem, st, L);                             \
   }
   FS_TUNE_LIST(FS_CASE)
   FS_TUNE_LIST_MODES(FS_CASE_M)
@@ -56,8 +83,7 @@ extern "C" int FS_RENDER_ENTRY(int op, const FsLaunch *L, const FsTune *t, int g
     }                                                                                      \
     if (op == 1) return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(occ, kern,      \
                                                                            TW_ * TPC_, smem); \
-    kern<<<grid, TW_ * TPC_, smem, st>>>(*L);                                              \
-    return (int)cudaGetLastError();                                                        \
+    return fs_launch(op, kern, grid, TW_ * TPC_, smem, st, L);                            \
   }
   FS_COOP_LIST(FS_COOP_CASE)
   FS_COOP_LIST_FX(FS_COOP_CASE_FX)

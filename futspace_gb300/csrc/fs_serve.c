@@ -414,8 +414,10 @@ static int launch_batch(fs_server *s, fs_slot *sl, fs_request *reqs, fs_fifo *re
   int32_t max_n = 0;
   for (int32_t i = 0; i < nb; i++)
     if (packed[i].n > max_n) max_n = packed[i].n;
-  if (!e) e = fsk_serve_prepare(packed_d, ids_d, nb, max_n, s->sess_d, s->zline, s->zinvz, sl->st);
+  /* the work counter is reset before the prologue kernel, so the render
+   * kernel (a programmatic dependent launch) follows that kernel directly */
   if (!e) e = cudaMemsetAsync(sl->head_d, 0, sizeof(int32_t), sl->st);
+  if (!e) e = fsk_serve_prepare(packed_d, ids_d, nb, max_n, s->sess_d, s->zline, s->zinvz, sl->st);
   if (!e) {
     FsLaunch L;
     memset(&L, 0, sizeof(L));
@@ -431,7 +433,7 @@ static int launch_batch(fs_server *s, fs_slot *sl, fs_request *reqs, fs_fifo *re
     const int32_t per_cta = fsk_items_per_cta(tune);
     const int32_t need = (ni + per_cta - 1) / per_cta;
     const int32_t grid = need < grid_max ? need : grid_max;
-    e = fsk_render(&L, tune, s->hf, s->cf, grid, sl->st);
+    e = fsk_render_pdl(&L, tune, s->hf, s->cf, grid, sl->st);
     ctx->launches += 2;
   }
   for (int32_t i = 0; i < nb && !e; i++) {

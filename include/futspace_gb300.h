@@ -127,11 +127,11 @@ int fs_ctx_force_tune(fs_ctx *ctx, const int32_t tune5[5]);
  * into segments marched by separate warps, after a pass that finds each
  * segment's minimum row; 0: never). Plans capture the options at creation or
  * retuning. Pixels are identical either way. Option "time" (0, default; 1:
- * record CUDA events around the render kernels of every plain per-frame call,
- * read with fs_ctx_kernel_ms) changes no pixel either. */
+ * record CUDA events around the kernels of every plain per-frame call, read
+ * with fs_ctx_kernel_ms) changes no pixel either. */
 int fs_ctx_set_option(fs_ctx *ctx, const char *name, int64_t value);
-/* Device time in ms of the render kernels (depth-table kernel excluded) of the
- * last plain per-frame call made with option "time" on; waits for that call.
+/* Device time in ms of the kernels (depth table and render) of the last plain
+ * per-frame call made with option "time" on; waits for that call.
  * FS_ERR_STATE when no such call was made. */
 int fs_ctx_kernel_ms(fs_ctx *ctx, float *ms);
 
