@@ -816,11 +816,14 @@ __global__ void __launch_bounds__(TW *LC, 1024 / (TW * LC)) segmin_kernel(
  * Phases C of block b-1 and A of block b run together, and block b+1's
  * depth-table entries load during B of block b (two buffers each), so a block
  * costs two barriers and its colour gathers overlap the next block's height
- * gathers. The column chain is one block per step instead of one chunk, so a
- * single frame with few columns keeps every SM busy. After the last block (or
- * once every column's minimum is row 0) the tile gets the forward fill and
- * sky. The stage is row-major, so every 32-row box of the tile goes to the
- * frame straight from it with TMA, all boxes back to back. */
+ * gathers. (Copying the next block's entries with cp.async while block b
+ * marches, into a third buffer, made the 1920x1080 frame 20 % slower.) The
+ * column chain is one block per step instead of one chunk, so a single frame
+ * with few columns keeps every SM busy. After the last block (or once every
+ * column's minimum is row 0) the tile gets the forward fill and sky, spread
+ * over all threads of the tile. The stage is row-major, so every 32-row box
+ * of the tile goes to the frame straight from it with TMA, all boxes back to
+ * back. */
 template <int TW, int TPC, int U>
 struct CoopShape {
   static constexpr int NT = TW * TPC;
@@ -900,6 +903,11 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int c = tid % TW; /* the thread's column within the tile (lane % TW) */
   const int j = tid / TW; /* its run within each depth block */
+  /* a plain call's view is a kernel parameter, so its stage can be filled
+   * with the gap value before the depth-table kernel has finished */
+  const bool param_view = !P.head && !P.items;
+  if (param_view)
+    for (int e = tid; e < P.view0.H * TW; e += NT) stage[e] = P.view0.gap;
   for (int i = tid; i < 256; i += NT) lut[i] = __fdiv_rn((float)i, 255.0f);
   wait_prior_grid();
   const LutChannels chan{lut};
@@ -969,11 +977,11 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
     /* a column past the frame's right edge starts (and stays) at row 0 */
     if (tid < TW) mcol[tid] = (c0 + tid < W) ? H : 0;
     if (tid == 0) scal[0] = scal[1] = 0;
-    for (int e = tid; e < H * TW; e += NT) stage[e] = gap;
+    if (!(param_view && iter == 0))
+      for (int e = tid; e < H * TW; e += NT) stage[e] = gap;
     load_table(0, 0);
     __syncthreads();
 
-    int fin = 1; /* which half of mcol holds the minima after the last block */
     for (int kb = 0, par = 0;; kb += NB, par ^= 1) {
       /* X: rows of block kb (A) with the colours of the previous block (C) */
       const int mstart = mcol[par * TW + c];
@@ -1032,8 +1040,16 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
        * block start holds no event; a warp of such runs skips the prefix,
        * except the last warp, which records the columns' new minima */
       if (warp == NW - 1 || __any_sync(FS_FULL_MASK, run < mstart)) {
+        /* the minimum over the earlier warps' totals of column c: the 32/TW
+         * lanes of the column read every (32/TW)-th warp each, then combine */
+        constexpr int Q = 32 / TW;
         int prev = mstart;
-        for (int w = 0; w < warp; w++) prev = min(prev, wtot[w * TW + c]);
+#pragma unroll
+        for (int w0 = 0; w0 < NW; w0 += Q)
+          if (w0 + lane / TW < warp) prev = min(prev, wtot[(w0 + lane / TW) * TW + c]);
+#pragma unroll
+        for (int off = TW; off < 32; off <<= 1)
+          prev = min(prev, __shfl_xor_sync(FS_FULL_MASK, prev, off));
         if (lane >= TW) prev = min(prev, ex);
         if (j == TPC - 1) mcol[(par ^ 1) * TW + c] = min(prev, run);
         int cnt = 0;
@@ -1083,18 +1099,47 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
       }
       if (done) {
         colour_events(par, kb);
-        fin = par ^ 1;
         break;
       }
     }
     __syncthreads();
 
-    /* forward fill + sky per column (a warp per column), then the tile store */
-    for (int cc = warp; cc < TW; cc += NW) {
-      const int mf = mcol[fin * TW + cc];
-      uint32_t *sc = stage + cc;
-      if (c0 + cc < W)
-        fill_column([sc](int y) { return sc + y * TW; }, 0, H, mf, gap, sky, lane);
+    /* fill_vline + sky (fut/voxel_renderer.fut:246-248) over the tile: thread
+     * (c, j) takes rows [j*R, j*R + R) of column c (R odd, so the column
+     * threads of a warp read distinct banks). Rows above a column's last
+     * event hold the gap value, so each row becomes the last non-gap value
+     * at or above it, or sky: the thread's last non-gap value, a scan of
+     * "the later non-gap value wins" over the column's threads (warp
+     * shuffles in steps of TW, then the warp totals), and a second pass. */
+    {
+      const int R = ((H + TPC - 1) / TPC) | 1;
+      const int ya = min(j * R, H), yz = min(ya + R, H);
+      uint32_t last = gap;
+      for (int y = ya; y < yz; y++) {
+        const uint32_t v = stage[y * TW + c];
+        if (v != gap) last = v;
+      }
+      uint32_t incl = last;
+#pragma unroll
+      for (int off = TW; off < 32; off <<= 1) {
+        const uint32_t t = __shfl_up_sync(FS_FULL_MASK, incl, off);
+        if (lane >= off && incl == gap) incl = t;
+      }
+      const uint32_t exw = __shfl_up_sync(FS_FULL_MASK, incl, TW);
+      uint32_t *const wlast = reinterpret_cast<uint32_t *>(wtot);
+      if (lane >= 32 - TW) wlast[warp * TW + c] = incl;
+      __syncthreads();
+      uint32_t carry = gap;
+      for (int w = 0; w < warp; w++) {
+        const uint32_t t = wlast[w * TW + c];
+        if (t != gap) carry = t;
+      }
+      if (lane >= TW && exw != gap) carry = exw;
+      for (int y = ya; y < yz; y++) {
+        const uint32_t v = stage[y * TW + c];
+        if (v != gap) carry = v;
+        stage[y * TW + c] = carry == gap ? sky : carry;
+      }
     }
     store_rows<TW, NT>(P, Vp, c0, stage, tid);
   }
