@@ -804,7 +804,8 @@ __global__ void __launch_bounds__(TW *LC, 1024 / (TW * LC)) segmin_kernel(
  * consecutive depths j*U .. j*U + U-1 of each block for column c. Per block b:
  *  A. every thread computes the rows of its U samples at once (all gathers in
  *     flight), unless a max-pyramid bound over its warp's columns and depths
- *     shows that none can be below the column minima at the block's start;
+ *     shows that none can be below the column minima at the block's start
+ *     (the bounds of 32 blocks come from one pass, a lane per block);
  *  B. the running minimum before each sample comes from a min-scan over the
  *     column's threads: the thread's own U rows, a warp scan (__shfl_up_sync
  *     in steps of TW lanes) and the warp totals in shared memory; events (row
@@ -982,7 +983,12 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
     load_table(0, 0);
     __syncthreads();
 
-    for (int kb = 0, par = 0;; kb += NB, par ^= 1) {
+    /* skip bounds of the warp's runs, 32 blocks at a time: lane l holds the
+     * bound of block bbase + l (its depth-table entries read from global
+     * memory), so one pass of the bound arithmetic and one round of
+     * max-pyramid loads serve 32 blocks */
+    int bbound = 0, bbase = -(1 << 30);
+    for (int kb = 0, par = 0, bi = 0;; kb += NB, par ^= 1, bi++) {
       /* X: rows of block kb (A) with the colours of the previous block (C) */
       const int mstart = mcol[par * TW + c];
       int r[U];
@@ -995,10 +1001,16 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
       const int ka = kb + jw * U, kz = min(kb + (jw + 32 / TW) * U, n) - 1;
       bool skip = ka > kz || __all_sync(FS_FULL_MASK, mstart == 0);
       if (!skip && M.pyr) {
-        const int ea = ka - kb, ez = kz - kb;
-        const int pa = (ea % U) * TPC + ea / U, pz = (ez % U) * TPC + ez / U;
-        const int b = box_row_bound(M, ztb[pa], zvb[pa], ztb[pz], zvb[pz], cam_h, horizon, H,
-                                    (float)c0, (float)max(c0, min(c0 + TW, W) - 1));
+        if (bi >= bbase + 32) {
+          bbase = bi;
+          const int kbl = (bi + lane) * NB;
+          const int kal = kbl + jw * U, kzl = min(kbl + (jw + 32 / TW) * U, n) - 1;
+          bbound = H + 1; /* past the last block: never consulted */
+          if (kal <= kzl)
+            bbound = chunk_row_bound(M, zl, zi, cam_h, horizon, H, (float)c0,
+                                     (float)max(c0, min(c0 + TW, W) - 1), kal, kzl);
+        }
+        const int b = __shfl_sync(FS_FULL_MASK, bbound, bi - bbase);
         skip = b >= (int)__reduce_max_sync(FS_FULL_MASK, (unsigned)mstart);
       }
       if (!skip && mstart > 0) {
