@@ -278,13 +278,15 @@ __device__ __forceinline__ uint32_t apply_effects(const Ch &ch, const FsView &V,
 }
 
 /* png_color_filtered, fut/render_functions.fut:95-105. Both x mixes share one
- * weight normalisation. */
-template <class Ch>
+ * weight normalisation. P2: the colour map's sides are powers of two (the
+ * wrap is a mask), known at compile time so the four index computations and
+ * gathers form one straight-line block. */
+template <bool P2, class Ch>
 __device__ __forceinline__ uint32_t color_bilinear(const FsMapDev &M, const Ch &ch, float x,
                                                    float y) {
   const float fx = floorf(x), cx = ceilf(x), fy = floorf(y), cy = ceilf(y);
-  const int32_t ix0 = wrap(f2i(fx), M.CW, M.cpow2), ix1 = wrap(f2i(cx), M.CW, M.cpow2);
-  const int32_t iy0 = wrap(f2i(fy), M.CH, M.cpow2), iy1 = wrap(f2i(cy), M.CH, M.cpow2);
+  const int32_t ix0 = wrap_t<P2>(f2i(fx), M.CW), ix1 = wrap_t<P2>(f2i(cx), M.CW);
+  const int32_t iy0 = wrap_t<P2>(f2i(fy), M.CH), iy1 = wrap_t<P2>(f2i(cy), M.CH);
   const uint32_t *r0 = M.c + (uint32_t)(iy0 * M.CW);
   const uint32_t *r1 = M.c + (uint32_t)(iy1 * M.CW);
   const uint32_t c00 = __ldg(r0 + ix0), c01 = __ldg(r0 + ix1);
@@ -303,9 +305,22 @@ __device__ __forceinline__ uint32_t color_bilinear(const FsMapDev &M, const Ch &
 }
 
 /* png_color, fut/render_functions.fut:91-92 */
+template <bool P2>
 __device__ __forceinline__ uint32_t color_nearest(const FsMapDev &M, float x, float y) {
-  const int32_t ix = wrap(f2i(x), M.CW, M.cpow2), iy = wrap(f2i(y), M.CH, M.cpow2);
+  const int32_t ix = wrap_t<P2>(f2i(x), M.CW), iy = wrap_t<P2>(f2i(y), M.CH);
   return __ldg(M.c + (uint32_t)(iy * M.CW) + ix);
+}
+__device__ __forceinline__ uint32_t color_nearest(const FsMapDev &M, float x, float y) {
+  return M.cpow2 ? color_nearest<true>(M, x, y) : color_nearest<false>(M, x, y);
+}
+
+/* The sample colour with the chosen filter (CF: bilinear), the wrap picked
+ * once per call from the colour map's shape. */
+template <int CF, class Ch>
+__device__ __forceinline__ uint32_t color_sample(const FsMapDev &M, const Ch &ch, bool p2,
+                                                 float x, float y) {
+  if (p2) return CF ? color_bilinear<true>(M, ch, x, y) : color_nearest<true>(M, x, y);
+  return CF ? color_bilinear<false>(M, ch, x, y) : color_nearest<false>(M, x, y);
 }
 
 }  // namespace fsd

@@ -333,7 +333,7 @@ __device__ __forceinline__ void render_strip(const FsLaunch &P, const FsView *Vp
     const float ec = (float)(c0 + ecl);
     const float4 L = __ldg(zl + k);
     const float2 xy = axpy2(ec, make_float2(L.z, L.w), make_float2(L.x, L.y));
-    uint32_t colour = CF ? color_bilinear(M, chan, xy.x, xy.y) : color_nearest(M, xy.x, xy.y);
+    uint32_t colour = color_sample<CF>(M, chan, M.cpow2 != 0, xy.x, xy.y);
     if constexpr (FX) {
       if (vflags & (FSV_SHADE | FSV_FOG)) {
         /* depth of sample k, as the depth table computes it */
@@ -953,7 +953,8 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
     };
     /* colour the events of the block in buffer half, each at its row */
     /* (kbc: the first depth of that block, for the optional epilogue) */
-    auto colour_events = [&](int half, int kbc) {
+    auto colour_list = [&](auto c2tag, int half, int kbc) {
+      constexpr bool C2 = decltype(c2tag)::value;
       const int ne = scal[half];
       if (P.stats && tid == 0) n_events += (uint32_t)ne;
       for (int e = tid; e < ne; e += NT) {
@@ -962,7 +963,8 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
         const float4 L = zt[half * NB + (kl % U) * TPC + kl / U];
         const float2 xy =
             axpy2((float)(c0 + ec), make_float2(L.z, L.w), make_float2(L.x, L.y));
-        uint32_t colour = CF ? color_bilinear(M, chan, xy.x, xy.y) : color_nearest(M, xy.x, xy.y);
+        uint32_t colour = CF ? color_bilinear<C2>(M, chan, xy.x, xy.y)
+                             : color_nearest<C2>(M, xy.x, xy.y);
         if constexpr (FX) {
           if (Vp->flags & (FSV_SHADE | FSV_FOG)) {
             /* depth of sample k, as the depth table computes it */
@@ -973,6 +975,13 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
         }
         stage[er * TW + ec] = colour;
       }
+    };
+    const bool cp2 = M.cpow2 != 0;
+    auto colour_events = [&](int half, int kbc) {
+      if (cp2)
+        colour_list(BoolTag<true>{}, half, kbc);
+      else
+        colour_list(BoolTag<false>{}, half, kbc);
     };
 
     /* a column past the frame's right edge starts (and stays) at row 0 */
