@@ -180,6 +180,38 @@ def test_non_power_of_two_map_and_i32_heights(fs, orc, gpu_ctx):
         assert count_diff(got, _oracle(orc, cam, p, hm, cm, 120, 90)) == 0
 
 
+@pytest.mark.parametrize("hf,cf", FILTERS)
+def test_non_power_of_two_map_every_configuration(fs, orc, gpu_ctx, hf, cf):
+    """Every compiled configuration (direct painting, staged tiles, cooperative
+    tiles) on a 300x200 map, whose height and colour wraps are the floored
+    modulo rather than a mask, for both filters, plus the smoothing and
+    shading/fog modes."""
+    hm = fs.gen_heights(13, 512, 0.6)[:300, :200].copy()
+    cm = fs.gen_colors(14, hm, 12)
+    fmap = fs.Map(gpu_ctx, hm, cm)
+    p = fs.default_params(height_filter=hf, color_filter=cf)
+    cams = fs.gen_cameras(15, hm, 2, above=(20, 80), distance=(250, 900), screen_h=61)
+    cams.append(fs.Camera(-450.25, 910.5, 140.0, 2.4, 30.0, 600.0, 1.1, 0xFF9090E0))
+    sizes = ((97, 61), (64, 130))
+    refs = {(i, w, h): _oracle(orc, c, p, hm, cm, w, h)
+            for i, c in enumerate(cams) for w, h in sizes}
+    try:
+        for tune in fs.tune_table():
+            gpu_ctx.force_tune(tune)
+            for (i, w, h), ref in refs.items():
+                got = gpu_ctx.render(fmap, cams[i], w, h, params=p)
+                assert count_diff(got, ref) == 0, (tune, i, w, h)
+    finally:
+        gpu_ctx.force_tune(None)
+    for extra in (dict(smoothing=1),
+                  dict(effects=3, shade=0.5, fog_start=50.0, fog_end=600.0,
+                       fog_color=0xFFA0B0C0)):
+        pm = fs.default_params(height_filter=hf, color_filter=cf, **extra)
+        for c in cams:
+            assert count_diff(gpu_ctx.render(fmap, c, 97, 61, params=pm),
+                              _oracle(orc, c, pm, hm, cm, 97, 61)) == 0, extra
+
+
 def test_chunk_skip_is_exact_and_saves_work(fs, orc, gpu_ctx):
     """The max-pyramid chunk skip changes no pixel and evaluates fewer samples."""
     hm = fs.gen_heights(17, 1024, 0.55)
