@@ -1127,9 +1127,9 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
 
     /* fill_vline + sky (fut/voxel_renderer.fut:246-248) over the tile: thread
      * (c, j) takes rows [j*R, j*R + R) of column c (R odd, so the column
-     * threads of a warp read distinct banks). Rows above a column's last
-     * event hold the gap value, so each row becomes the last non-gap value
-     * at or above it, or sky: the thread's last non-gap value, a scan of
+     * threads of a warp read distinct banks). Rows no event wrote still
+     * hold the gap value, so each row becomes the last non-gap value at or
+     * above it, or sky: the thread's last non-gap value, a scan of
      * "the later non-gap value wins" over the column's threads (warp
      * shuffles in steps of TW, then the warp totals), and a second pass. */
     {
