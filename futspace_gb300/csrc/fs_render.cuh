@@ -836,7 +836,7 @@ struct CoopShape {
   static constexpr size_t zi_bytes = 2ull * NB * 4;
   static constexpr size_t ev_bytes = 2ull * ECAP * 4; /* two blocks' event lists */
   /* warp totals [NW][TW], block-start minima [2][TW], event counts [2], item */
-  static constexpr size_t misc_bytes = ((size_t)NW * TW + 2 * TW + 3) * 4;
+  static constexpr size_t misc_bytes = ((size_t)NW * TW + 2 * TW + 4) * 4;
   /* the stage starts on a 128-byte boundary, as do its boxes (TMA sources) */
   static constexpr size_t fixed_bytes =
       (lut_bytes + zl_bytes + zi_bytes + ev_bytes + misc_bytes + 127) / 128 * 128;
@@ -889,6 +889,7 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
   constexpr int NT = S::NT, NW = S::NW, NB = S::NB, ECAP = S::ECAP;
   static_assert(TW >= 4 && 32 % TW == 0 && NT % 32 == 0, "a warp holds whole runs of TW columns");
   static_assert(NB <= 2048 && TW <= 32, "event fields");
+  static_assert(NB % NT == 0, "a block's depth-table entries split evenly over the threads");
 
   extern __shared__ __align__(1024) unsigned char smem[];
   float *lut = reinterpret_cast<float *>(smem);
@@ -898,7 +899,9 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
   int *wtot =
       reinterpret_cast<int *>(smem + S::lut_bytes + S::zl_bytes + S::zi_bytes + S::ev_bytes);
   int *mcol = wtot + NW * TW;
-  int *scal = mcol + 2 * TW; /* [0], [1] events of the even / odd block, [2] next item */
+  /* [0], [1] events of the even / odd block, [2] next item, [3] every column
+   * at row 0 after the block */
+  int *scal = mcol + 2 * TW;
   uint32_t *stage = reinterpret_cast<uint32_t *>(smem + S::fixed_bytes);
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -907,10 +910,23 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
   /* a plain call's view is a kernel parameter, so its stage can be filled
    * with the gap value before the depth-table kernel has finished */
   const bool param_view = !P.head && !P.items;
-  if (param_view)
+  if (param_view) {
     for (int e = tid; e < P.view0.H * TW; e += NT) stage[e] = P.view0.gap;
+    /* block 0's depth-table entries straight from the camera, as the
+     * depth-table kernel computes them, so the march starts before that
+     * kernel has finished; its results are read from block 1 on */
+    const DepthLine dl(P.view0);
+    for (int p = tid; p < NB; p += NT) {
+      const int e = (p % TPC) * U + p / TPC;
+      float4 L = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+      float iz = 0.0f;
+      if (e < P.view0.n) dl.entry(e, L, iz);
+      zt[p] = L;
+      zv[p] = iz;
+    }
+  }
   for (int i = tid; i < 256; i += NT) lut[i] = __fdiv_rn((float)i, 255.0f);
-  wait_prior_grid();
+  if (!param_view) wait_prior_grid();
   const LutChannels chan{lut};
   uint32_t n_samples = 0, n_events = 0;
 
@@ -987,9 +1003,10 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
     /* a column past the frame's right edge starts (and stays) at row 0 */
     if (tid < TW) mcol[tid] = (c0 + tid < W) ? H : 0;
     if (tid == 0) scal[0] = scal[1] = 0;
-    if (!(param_view && iter == 0))
+    if (!(param_view && iter == 0)) {
       for (int e = tid; e < H * TW; e += NT) stage[e] = gap;
-    load_table(0, 0);
+      load_table(0, 0);
+    }
     __syncthreads();
 
     /* skip bounds of the warp's runs, 32 blocks at a time: lane l holds the
@@ -1010,16 +1027,25 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
       const int ka = kb + jw * U, kz = min(kb + (jw + 32 / TW) * U, n) - 1;
       bool skip = ka > kz || __all_sync(FS_FULL_MASK, mstart == 0);
       if (!skip && M.pyr) {
-        if (bi >= bbase + 32) {
-          bbase = bi;
-          const int kbl = (bi + lane) * NB;
-          const int kal = kbl + jw * U, kzl = min(kbl + (jw + 32 / TW) * U, n) - 1;
-          bbound = H + 1; /* past the last block: never consulted */
-          if (kal <= kzl)
-            bbound = chunk_row_bound(M, zl, zi, cam_h, horizon, H, (float)c0,
-                                     (float)max(c0, min(c0 + TW, W) - 1), kal, kzl);
+        const float cf = (float)c0, cl = (float)max(c0, min(c0 + TW, W) - 1);
+        int b;
+        if (param_view && bi == 0) {
+          /* a plain call's block 0 marches before the depth-table kernel has
+           * finished: its bound comes from the entries in shared memory */
+          const int ea = ka - kb, ez = kz - kb;
+          const int pa = (ea % U) * TPC + ea / U, pz = (ez % U) * TPC + ez / U;
+          b = box_row_bound(M, ztb[pa], zvb[pa], ztb[pz], zvb[pz], cam_h, horizon, H, cf, cl);
+        } else {
+          if (bi >= bbase + 32) {
+            bbase = bi;
+            const int kbl = (bi + lane) * NB;
+            const int kal = kbl + jw * U, kzl = min(kbl + (jw + 32 / TW) * U, n) - 1;
+            bbound = H + 1; /* past the last block: never consulted */
+            if (kal <= kzl)
+              bbound = chunk_row_bound(M, zl, zi, cam_h, horizon, H, cf, cl, kal, kzl);
+          }
+          b = __shfl_sync(FS_FULL_MASK, bbound, bi - bbase);
         }
-        const int b = __shfl_sync(FS_FULL_MASK, bbound, bi - bbase);
         skip = b >= (int)__reduce_max_sync(FS_FULL_MASK, (unsigned)mstart);
       }
       if (!skip && mstart > 0) {
@@ -1053,6 +1079,22 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
       }
       const int ex = __shfl_up_sync(FS_FULL_MASK, incl, TW);
       if (lane >= 32 - TW) wtot[warp * TW + c] = incl;
+      /* the next block's depth-table entries: loaded here, stored to shared
+       * memory at the end of B, so the loads' latency overlaps the barrier */
+      if (param_view && kb == 0) wait_prior_grid();
+      const bool more = kb + NB < n;
+      float4 Lnext[NB / NT];
+      float iznext[NB / NT];
+#pragma unroll
+      for (int q = 0; q < NB / NT; q++) {
+        const int p = tid + q * NT, e = (p % TPC) * U + p / TPC;
+        Lnext[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        iznext[q] = 0.0f;
+        if (kb + NB + e < n) {
+          Lnext[q] = __ldg(zl + kb + NB + e);
+          iznext[q] = __ldg(zi + kb + NB + e);
+        }
+      }
       __syncthreads();
 
       /* Y: the minimum before each sample, the block's events (B), and the
@@ -1073,6 +1115,10 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
           prev = min(prev, __shfl_xor_sync(FS_FULL_MASK, prev, off));
         if (lane >= TW) prev = min(prev, ex);
         if (j == TPC - 1) mcol[(par ^ 1) * TW + c] = min(prev, run);
+        if (warp == NW - 1) {
+          const bool z = __all_sync(FS_FULL_MASK, lane < 32 - TW || min(prev, run) == 0);
+          if (lane == 31) scal[3] = z;
+        }
         int cnt = 0;
         if (run < prev) {
           int pv = prev;
@@ -1105,19 +1151,19 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
           }
         }
       }
-      const bool more = kb + NB < n;
-      if (more) load_table(kb + NB, par ^ 1);
+      if (more) {
+#pragma unroll
+        for (int q = 0; q < NB / NT; q++) {
+          zt[(par ^ 1) * NB + tid + q * NT] = Lnext[q];
+          zv[(par ^ 1) * NB + tid + q * NT] = iznext[q];
+        }
+      }
       if (tid == 0) scal[par ^ 1] = 0; /* the previous block's list is coloured */
       __syncthreads();
 
       /* the last block, or every column at row 0: colour it and finish */
       bool done = !more;
-      if (more) {
-        bool all0 = true;
-#pragma unroll
-        for (int cc = 0; cc < TW; cc++) all0 = all0 && mcol[(par ^ 1) * TW + cc] == 0;
-        done = all0;
-      }
+      if (more) done = scal[3] != 0;
       if (done) {
         colour_events(par, kb);
         break;
