@@ -815,9 +815,11 @@ __global__ void __launch_bounds__(TW *LC, 1024 / (TW * LC)) segmin_kernel(
  *     is the reference's scatter (fut/voxel_renderer.fut:244); its forward fill
  *     (:246) runs once over the finished tile.
  * Phases C of block b-1 and A of block b run together, and block b+1's
- * depth-table entries load during B of block b (two buffers each), so a block
- * costs two barriers and its colour gathers overlap the next block's height
- * gathers. (Copying the next block's entries with cp.async while block b
+ * depth-table entries load into registers at the end of A and go to shared
+ * memory during B (two buffers each), so a block costs two barriers and its
+ * colour gathers overlap the next block's height gathers. A plain call (the
+ * view is a kernel parameter) computes block 0's entries in the CTA and
+ * marches it while the depth-table kernel finishes. (Copying the next block's entries with cp.async while block b
  * marches, into a third buffer, made the 1920x1080 frame 20 % slower.) The
  * column chain is one block per step instead of one chunk, so a single frame
  * with few columns keeps every SM busy. After the last block (or once every
