@@ -819,10 +819,11 @@ __global__ void __launch_bounds__(TW *LC, 1024 / (TW * LC)) segmin_kernel(
  * memory during B (two buffers each), so a block costs two barriers and its
  * colour gathers overlap the next block's height gathers. A plain call (the
  * view is a kernel parameter) computes block 0's entries in the CTA and
- * marches it while the depth-table kernel finishes. (Copying the next block's entries with cp.async while block b
- * marches, into a third buffer, made the 1920x1080 frame 20 % slower.) The
- * column chain is one block per step instead of one chunk, so a single frame
- * with few columns keeps every SM busy. After the last block (or once every
+ * marches it while the depth-table kernel finishes. (Copying the next
+ * block's entries with cp.async while block b marches, into a third buffer,
+ * made the 1920x1080 frame 20 % slower.) The column chain is one block per
+ * step instead of one chunk, so a single frame with few columns keeps every
+ * SM busy. After the last block (or once every
  * column's minimum is row 0) the tile gets the forward fill and sky, spread
  * over all threads of the tile. The stage is row-major, so every 32-row box
  * of the tile goes to the frame straight from it with TMA, all boxes back to
