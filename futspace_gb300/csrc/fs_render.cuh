@@ -823,11 +823,10 @@ __global__ void __launch_bounds__(TW *LC, 1024 / (TW * LC)) segmin_kernel(
  * block's entries with cp.async while block b marches, into a third buffer,
  * made the 1920x1080 frame 20 % slower.) The column chain is one block per
  * step instead of one chunk, so a single frame with few columns keeps every
- * SM busy. After the last block (or once every
- * column's minimum is row 0) the tile gets the forward fill and sky, spread
- * over all threads of the tile. The stage is row-major, so every 32-row box
- * of the tile goes to the frame straight from it with TMA, all boxes back to
- * back. */
+ * SM busy. After the last block (or once every column's minimum is row 0)
+ * the tile gets the forward fill and sky, spread over all threads of the
+ * tile. The stage is row-major, so every 32-row box of the tile goes to the
+ * frame straight from it with TMA, all boxes back to back. */
 template <int TW, int TPC, int U>
 struct CoopShape {
   static constexpr int NT = TW * TPC;
