@@ -190,6 +190,15 @@ int fs_ctx_new(fs_ctx **out, int32_t device) {
     return fs_fail(ctx, FS_ERR_NOMEM, "cudaMalloc(stats)");
   }
   cudaMemset(ctx->stats_dev, 0, 2 * sizeof(unsigned long long));
+  /* the allocation-free render's scratch address: looking it up may load the
+   * library's module onto the device (which allocates its fixed arrays), so
+   * it happens here, in a call that allocates anyway, and never in a render */
+  e = fs_noalloc_setup(ctx);
+  if (e) {
+    ctx->broken = 1;
+    *out = ctx;
+    return e;
+  }
   fs_tune_cache_load(ctx);
   *out = ctx;
   return FS_OK;

@@ -22,9 +22,12 @@
  *    them (nothing needs to start at zero), so calls that overlap on the GPU --
  *    on different streams or contexts of the same device -- race and must be
  *    serialised by the caller;
- *  - the first call on a device looks up the array's device address
- *    (cudaGetSymbolAddress, a one-time set-up with that device current); make
- *    that first call before any stream capture.
+ *  - the array's device address is looked up once per context, with the
+ *    context's device current, when fs_ctx_new creates it (cudaGetSymbolAddress:
+ *    the first lookup on a device may load this library's module there, which
+ *    is when the array itself is allocated). So no render call loads a module
+ *    or allocates, and no render call depends on state shared between host
+ *    threads.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -38,20 +41,14 @@
 #define FS_NOALLOC_ENTRIES (FS_NOALLOC_MAX_DEPTHS + FS_ZPAD)
 static __device__ __align__(256) unsigned char fs_noalloc_scratch[FS_NOALLOC_ENTRIES * 20];
 
-/* Device address of fs_noalloc_scratch per device ordinal. In host code the
- * array's name only stands in for it; the kernels must be given this address. */
-static void *g_scratch_dev[64];
-
-static int scratch_address(fs_ctx *ctx, void **out) {
-  if (ctx->device < 0 || ctx->device >= 64)
-    return fs_fail(ctx, FS_ERR_ARG, "device ordinal %d out of range", ctx->device);
-  if (!g_scratch_dev[ctx->device]) {
-    void *p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, fs_noalloc_scratch);
-    if (e != cudaSuccess) return fs_cuda_fail(ctx, (int)e, "cudaGetSymbolAddress(scratch)");
-    g_scratch_dev[ctx->device] = p;
-  }
-  *out = g_scratch_dev[ctx->device];
+/* In host code the array's name only stands in for it: the kernels must be
+ * given its device address, which this looks up on the current device (the
+ * context's) and keeps in the context. */
+extern "C" int fs_noalloc_setup(fs_ctx *ctx) {
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, fs_noalloc_scratch);
+  if (e != cudaSuccess) return fs_cuda_fail(ctx, (int)e, "cudaGetSymbolAddress(scratch)");
+  ctx->noalloc_scratch = p;
   return FS_OK;
 }
 
@@ -72,9 +69,8 @@ extern "C" int fs_render_device_noalloc(fs_ctx *ctx, const fs_map *map, const fs
                    v.n, FS_NOALLOC_MAX_DEPTHS);
   const cudaError_t e = cudaSetDevice(ctx->device);
   if (e != cudaSuccess) return fs_cuda_fail(ctx, (int)e, "cudaSetDevice");
-  void *scratch = nullptr;
-  rc = scratch_address(ctx, &scratch);
-  if (rc) return rc;
+  void *const scratch = ctx->noalloc_scratch;
+  if (!scratch) return fs_fail(ctx, FS_ERR_STATE, "allocation-free scratch not set up");
   float4 *zline = reinterpret_cast<float4 *>(scratch);
   float *zinvz = reinterpret_cast<float *>(static_cast<unsigned char *>(scratch) +
                                            sizeof(float4) * FS_NOALLOC_ENTRIES);

@@ -43,6 +43,9 @@ struct fs_ctx {
   int32_t time_kernel;   /* 1: events around the render kernels of each plain call */
   int32_t kernel_timed;  /* the events hold a completed call's timing */
   cudaEvent_t ev_kernel[2];
+  /* device address of the allocation-free render's fixed scratch array on
+   * this context's device, looked up once at context creation */
+  void *noalloc_scratch;
   FsTune forced; /* tw == 0: choose per frame */
   int32_t ntune;
   fs_tune_entry tunes[FS_TUNE_CACHE_MAX];
@@ -106,6 +109,9 @@ struct fs_plan {
 };
 
 int fs_fail(fs_ctx *ctx, int code, const char *fmt, ...);
+/* Looks up the allocation-free render's scratch address on ctx's (current)
+ * device into ctx->noalloc_scratch (fs_noalloc.cu). */
+int fs_noalloc_setup(fs_ctx *ctx);
 int fs_cuda_fail(fs_ctx *ctx, int e, const char *what);
 int32_t fs_f2i_host(float v);
 int fs_check_params(fs_ctx *ctx, const fs_params *p);

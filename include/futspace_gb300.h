@@ -182,8 +182,9 @@ int fs_render(fs_ctx *ctx, const fs_map *map, const fs_camera *cam, const fs_par
  * a fixed 1.25 MiB array compiled into the library (held on every GPU that
  * loads the library until exit), so a frame may use at most 65536 depth
  * samples; longer schedules fail with FS_ERR_ARG. All calls share that array:
- * calls that overlap on the GPU race. The first call on a device looks up the
- * array's address (one-time set-up); make it before any stream capture. */
+ * calls that overlap on the GPU race. The array's device address is looked up
+ * once, by fs_ctx_new (which may load the library's module onto the device and
+ * so allocate the array there), so the render calls themselves do no set-up. */
 int fs_render_device_noalloc(fs_ctx *ctx, const fs_map *map, const fs_camera *cam,
                              const fs_params *params, int32_t width, int32_t height,
                              uint32_t *out_dev);

@@ -14,6 +14,16 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (sm_103a)")
 
 
+def reference_dir():
+    """A checkout of the reference project (MrHootJones/futspace), named by the
+    environment variable FUTSPACE_REFERENCE_DIR; None when it is not set or
+    does not exist (the tests that read its files then skip)."""
+    p = os.environ.get("FUTSPACE_REFERENCE_DIR")
+    if not p or not Path(p).is_dir():
+        return None
+    return Path(p)
+
+
 @pytest.fixture(scope="session", autouse=True)
 def _tune_cache(tmp_path_factory):
     # keep tuning-cache writes out of the working tree

@@ -12,7 +12,10 @@ from pathlib import Path
 import numpy as np
 import pytest
 
-REF = Path("/root/reference")
+from conftest import reference_dir
+
+# the reference checkout (FUTSPACE_REFERENCE_DIR), None when absent
+REF = reference_dir()
 
 
 # ---- an independent PNG encoder/decoder in numpy + zlib (test side) ----------
@@ -195,7 +198,8 @@ def test_png_write_round_trip(fs, tmp_path):
     np.testing.assert_array_equal(fs.png_read(p), big | np.uint32(0xFF000000))
 
 
-@pytest.mark.skipif(not (REF / "data").exists(), reason="reference map images not present")
+@pytest.mark.skipif(REF is None or not (REF / "data").exists(),
+                    reason="reference map images not present (set FUTSPACE_REFERENCE_DIR)")
 @pytest.mark.parametrize("name", ["converted-maps/C1W.png", "converted-maps/D1.png",
                                   "unconverted-maps/C1W.png", "unconverted-maps/D1.png",
                                   "custom-maps/testmap.png"])
@@ -212,9 +216,9 @@ def test_png_decode_reference_maps(fs, name):
 def _reference_data_reader():
     """tools/data2png.py's read_image, imported with its image-writing module
     stubbed out (only the reader is used)."""
+    if REF is None or not (REF / "tools" / "data2png.py").exists():
+        pytest.skip("reference tools not present (set FUTSPACE_REFERENCE_DIR)")
     path = REF / "tools" / "data2png.py"
-    if not path.exists():
-        pytest.skip("reference tools not present")
     sys.modules.setdefault("png", types.ModuleType("png"))
     spec = importlib.util.spec_from_file_location("ref_data2png", path)
     mod = importlib.util.module_from_spec(spec)
