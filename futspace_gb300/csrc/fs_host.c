@@ -212,12 +212,6 @@ void fs_ctx_free(fs_ctx *ctx) {
   cudaFree(ctx->zinvz);
   cudaFree(ctx->frame_dev);
   cudaFree(ctx->segbuf);
-  cudaFree(ctx->pipe.rows);
-  cudaFree(ctx->pipe.segmin);
-  cudaFree(ctx->pipe.events);
-  cudaFree(ctx->pipe.count);
-  cudaFree(ctx->pipe.colmin);
-  cudaFree(ctx->pipe.flags);
   cudaFree(ctx->stats_dev);
   if (ctx->ev_kernel[0]) cudaEventDestroy(ctx->ev_kernel[0]);
   if (ctx->ev_kernel[1]) cudaEventDestroy(ctx->ev_kernel[1]);
@@ -554,7 +548,6 @@ static const FsTune k_tune_order[] = {
     {32, 8, 4, 0, 0},  {32, 4, 4, 0, 0},  {64, 4, 4, 0, 0},  {32, 4, 8, 0, 0},
     {64, 2, 4, 0, 0},  {64, 1, 4, 0, 0},  {128, 1, 4, 0, 0}, {64, 1, 8, 0, 0},
     {128, 1, 8, 0, 0}, {4, 64, 8, 2, 0},  {8, 32, 8, 2, 0},  {4, 64, 4, 2, 0},
-    {32, 1, 64, 3, 0},
 };
 
 int fs_tune_count(void) { return (int)(sizeof(k_tune_order) / sizeof(k_tune_order[0])); }
@@ -585,68 +578,6 @@ FsTune fs_tune_for_mode(FsTune t, int32_t view_flags) {
     t = d;
   }
   return t;
-}
-
-/* The first table entry other than the row pipeline that fits: for calls
- * that may use no scratch beyond the depth table. */
-static FsTune default_tune_without_pipe(fs_ctx *ctx, int32_t stride_max) {
-  for (int i = 0; i < fs_tune_count(); i++)
-    if (k_tune_order[i].stage != 3 && fs_tune_fits(ctx, &k_tune_order[i], stride_max))
-      return k_tune_order[i];
-  FsTune none = {0, 0, 0, 0, 0};
-  return none;
-}
-
-/* Grows one scratch buffer of the context to hold `need` elements of `size`
- * bytes (stream-synchronised free of the old one). */
-static int grow_scratch(fs_ctx *ctx, void **buf, int64_t *cap, int64_t need, size_t size,
-                        const char *what) {
-  if (need <= *cap) return FS_OK;
-  cudaStreamSynchronize(ctx->stream);
-  cudaFree(*buf);
-  *buf = NULL;
-  *cap = 0;
-  if (cudaMalloc(buf, size * (size_t)need) != cudaSuccess)
-    return fs_fail(ctx, FS_ERR_NOMEM, "cudaMalloc(%s)", what);
-  *cap = need;
-  return FS_OK;
-}
-
-/* Row-pipeline scratch for a W-column frame of n depths and H rows: rows
- * [W][n rounded up to whole segments], segment minima [W][segments rounded
- * up to 8], and at most min(n, H) events per column (each event lowers the
- * column's minimum row). */
-static int ensure_pipe(fs_ctx *ctx, int32_t W, int32_t n, int32_t H) {
-  FsPipe *Q = &ctx->pipe;
-  const int32_t nseg = (n + FS_PIPE_SEG - 1) / FS_PIPE_SEG;
-  const int32_t rpitch = nseg * FS_PIPE_SEG, spitch = (nseg + 7) / 8 * 8;
-  const int64_t ecap = (int64_t)W * (n < H ? n : H);
-  int rc = grow_scratch(ctx, (void **)&Q->rows, &ctx->pipe_rows_cap, (int64_t)W * rpitch, 2,
-                        "pipeline rows");
-  if (!rc)
-    rc = grow_scratch(ctx, (void **)&Q->segmin, &ctx->pipe_seg_cap, (int64_t)W * spitch, 2,
-                      "pipeline segment minima");
-  if (!rc)
-    rc = grow_scratch(ctx, (void **)&Q->events, &ctx->pipe_ev_cap, ecap,
-                      sizeof(unsigned long long), "pipeline events");
-  if (!rc && !Q->count) {
-    if (cudaMalloc((void **)&Q->count, 64) != cudaSuccess)
-      rc = fs_fail(ctx, FS_ERR_NOMEM, "cudaMalloc(pipeline counter)");
-  }
-  if (!rc && (int64_t)W > ctx->pipe_col_cap) {
-    int64_t cap = ctx->pipe_col_cap;
-    rc = grow_scratch(ctx, (void **)&Q->colmin, &cap, W, sizeof(int32_t), "pipeline columns");
-    cap = ctx->pipe_col_cap;
-    if (!rc) rc = grow_scratch(ctx, (void **)&Q->flags, &cap, W, sizeof(int32_t),
-                               "pipeline column flags");
-    if (!rc) ctx->pipe_col_cap = W;
-  }
-  if (rc) return rc;
-  Q->ecap = ecap;
-  Q->rpitch = rpitch;
-  Q->spitch = spitch;
-  Q->nseg = nseg;
-  return FS_OK;
 }
 
 /* Default choice when the tuning cache has no entry: the first table entry
@@ -703,42 +634,8 @@ int fs_render_view(fs_ctx *ctx, const FsMapDev *map, FsView *v, const FsTune *tu
   t = fs_tune_for_mode(t, v->flags);
   if (!t.tw || !fs_tune_fits(ctx, &t, stride))
     return fs_fail(ctx, FS_ERR_ARG, "no kernel configuration fits screen height %d", v->H);
-  if (t.stage == 3 && !allow_split) {
-    /* the row pipeline needs the context's scratch: the caller allows none */
-    t = fs_tune_for_mode(default_tune_without_pipe(ctx, stride), v->flags);
-    if (!t.tw || !fs_tune_fits(ctx, &t, stride))
-      return fs_fail(ctx, FS_ERR_ARG, "no kernel configuration fits screen height %d", v->H);
-  }
   const int32_t hf = (v->flags & FSV_HEIGHT_BILINEAR) != 0;
   const int32_t cf = (v->flags & FSV_COLOR_BILINEAR) != 0;
-  if (t.stage == 3) {
-    /* the row pipeline: depth table, rows, events, colour and paint, gap fill */
-    int rc = ensure_pipe(ctx, v->W, v->n, v->H);
-    if (rc) return rc;
-    v->tmap = -1;
-    v->nseg = 1;
-    v->segbuf = NULL;
-    FsLaunch launch;
-    memset(&launch, 0, sizeof(launch));
-    launch.view0 = *v;
-    launch.view0.map = 0;
-    launch.maps[0] = *map;
-    launch.zline = zline;
-    launch.zinvz = zinvz;
-    launch.stats = ctx->stats_dev;
-    launch.stride_max = stride;
-    if (ctx->time_kernel) cudaEventRecord(ctx->ev_kernel[0], ctx->stream);
-    int e = fsk_ztable(NULL, &launch.view0, 1, v->n, zline, zinvz, ctx->stream);
-    if (e) return fs_cuda_fail(ctx, e, "z-table kernel launch");
-    e = fsk_pipe(&launch, &ctx->pipe, hf, cf, t.fx, ctx->sm_count, ctx->stream);
-    if (e) return fs_cuda_fail(ctx, e, "row pipeline launch");
-    ctx->launches += 5;
-    if (ctx->time_kernel) {
-      cudaEventRecord(ctx->ev_kernel[1], ctx->stream);
-      ctx->kernel_timed = 1;
-    }
-    return FS_OK;
-  }
   const int32_t iw = fsk_item_width(&t), ntiles = (v->W + iw - 1) / iw;
   const int32_t per_cta = fsk_items_per_cta(&t);
   /* a frame with few strips splits each column's depths over several warps */

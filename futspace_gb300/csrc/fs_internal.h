@@ -115,22 +115,6 @@ typedef struct {
   int32_t seg;    /* 1: kernels that read depth segments (some view is split) */
 } FsTune;
 
-/* Scratch of the row pipeline (tuning stage 3, fs_pipe.cu) for one plain
- * call: every depth sample's screen row, per-segment minimum rows, the
- * frame's occlusion events and per-column results. Segments are FS_PIPE_SEG
- * consecutive depths. */
-#define FS_PIPE_SEG 64
-typedef struct {
-  uint16_t *rows;             /* [W][rpitch]: row of depth k of column c, H past n */
-  uint16_t *segmin;           /* [W][spitch]: minimum row of each segment */
-  unsigned long long *events; /* ecap packed events (fs_pipe.cu: pack_pipe_event) */
-  int32_t *count;             /* [0]: events of the frame */
-  int32_t *colmin;            /* [W]: each column's final minimum row */
-  int32_t *flags;             /* [W]: 1 when the column painted the gap colour */
-  int64_t ecap;
-  int32_t rpitch, spitch, nseg, pad;
-} FsPipe;
-
 /* Kernel-side entry points (fs_kernels.cu). Each returns a cudaError_t. */
 int fsk_ztable(const FsView *views_dev, const FsView *view0, int32_t nviews, int32_t max_n,
                float4 *zline, float *zinvz, cudaStream_t st);
@@ -149,10 +133,6 @@ int fsk_segmin(const FsLaunch *L, const FsTune *t, int32_t hf, int32_t grid, cud
 int fsk_gapfill(const FsView *views_dev, const FsView *view0, int32_t nviews, int32_t max_w,
                 cudaStream_t st);
 int32_t fsk_items_per_cta(const FsTune *t);
-/* The row pipeline of a plain call's view0 (fs_pipe.cu): rows, events,
- * colour and paint, gap fill; every kernel a programmatic dependent launch. */
-int fsk_pipe(const FsLaunch *L, const FsPipe *Q, int32_t hf, int32_t cf, int32_t fx,
-             int32_t sm_count, cudaStream_t st);
 int fsk_l2_read(const void *buf, int64_t bytes, int32_t reps, int32_t grid, uint32_t *sink,
                 cudaStream_t st);
 /* A work item names a view (or serving session), a depth segment and a column

@@ -191,8 +191,6 @@ extern "C" int fsk_tune_supported(const FsTune *t) {
 #define FS_CASE_CF(TW_, TPC_, U_)                                                    \
   if (t->stage == 2 && t->tw == TW_ && t->lc == TPC_ && t->u == U_ && !t->smooth && t->fx) \
     return 1;
-  /* the row pipeline (fs_pipe.cu): plain mode or the epilogue */
-  if (t->stage == 3 && t->tw == 32 && t->lc == 1 && t->u == FS_PIPE_SEG && !t->smooth) return 1;
   FS_TUNE_LIST(FS_CASE)
   FS_TUNE_LIST_MODES(FS_CASE_M)
   FS_COOP_LIST(FS_CASE_C)
@@ -205,7 +203,6 @@ extern "C" int fsk_tune_supported(const FsTune *t) {
 }
 
 extern "C" size_t fsk_render_smem(const FsTune *t, int32_t stride_max) {
-  if (t->stage == 3) return 0; /* the row pipeline's kernels use static shared memory */
 #define FS_COOP_SMEM(TW_, TPC_, U_)                                  \
   if (t->stage == 2 && t->tw == TW_ && t->lc == TPC_ && t->u == U_) \
     return CoopShape<TW_, TPC_, U_>::fixed_bytes + CoopShape<TW_, TPC_, U_>::stage_bytes(stride_max);

@@ -565,8 +565,6 @@ int fs_plan_get_tune(const fs_plan *p, int32_t out5[5]) {
 int fs_plan_set_tune(fs_plan *p, const int32_t tune5[5]) {
   if (!p || !tune5) return FS_ERR_ARG;
   FsTune t = {tune5[0], tune5[1], tune5[2], tune5[3], tune5[4], 0, 0};
-  if (t.stage == 3)
-    return fs_fail(p->ctx, FS_ERR_ARG, "the row pipeline (stage 3) renders plain calls only");
   t.smooth = (p->fv_h[0].flags & FSV_SMOOTH) ? 1 : 0;
   t.fx = (p->fv_h[0].flags & (FSV_SHADE | FSV_FOG)) ? 1 : 0;
   if (!fs_tune_fits(p->ctx, &t, p->stride_max))

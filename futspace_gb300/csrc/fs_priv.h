@@ -37,8 +37,6 @@ struct fs_ctx {
   int64_t segcap;
   uint32_t *frame_dev; /* device frame for fs_render with host output */
   size_t frame_cap;
-  FsPipe pipe; /* row-pipeline scratch (tuning stage 3) for plain calls */
-  int64_t pipe_rows_cap, pipe_seg_cap, pipe_ev_cap, pipe_col_cap; /* elements held */
   unsigned long long *stats_dev;
   int32_t collect_stats;
   int64_t launches;
@@ -122,9 +120,6 @@ int fs_make_view(fs_ctx *ctx, const fs_camera *cam, const fs_params *p, int32_t 
 int fs_ensure_ztable(fs_ctx *ctx, int64_t n);
 int fs_encode_frame_map(fs_ctx *ctx, uint32_t *frame, int32_t W, int32_t H, int32_t tw,
                         CUtensorMap *out);
-/* Renders view v (v->out set) with its depth table in zline/zinvz. allow_split
- * 1: the call may use the context's own scratch buffers (depth segments, the
- * row pipeline); 0: none beyond the depth table it is given. */
 int fs_render_view(fs_ctx *ctx, const FsMapDev *map, FsView *v, const FsTune *tune,
                    float4 *zline, float *zinvz, const CUtensorMap *tmap_pre, int32_t allow_split);
 int32_t fs_split_target(fs_ctx *ctx, const FsTune *t, int32_t hf, int32_t cf, int32_t stride,

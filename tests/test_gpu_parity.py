@@ -91,10 +91,7 @@ def test_batch_plan_all_configurations(fs, orc, gpu_ctx, maps1024):
     p = fs.default_params()
     refs = [_oracle(orc, c, p, hm, cm, w, h) for c, w, h in views]
     plan = fs.Plan(gpu_ctx, [fmap], views)
-    batch_tunes = [t for t in fs.tune_table() if t[3] != 3]  # the row pipeline: plain calls
-    with pytest.raises(fs.FsError):
-        plan.set_tune(32, 1, 64, 3)
-    for tune in batch_tunes:
+    for tune in fs.tune_table():
         plan.set_tune(*tune)
         plan.run()
         frames = plan.frames()
@@ -109,7 +106,7 @@ def test_batch_plan_all_configurations(fs, orc, gpu_ctx, maps1024):
         flat = plan.run_download(buf.array, groups=groups)
         bad = [i for i, (f, r) in enumerate(zip(plan.frames(flat), refs)) if count_diff(f, r)]
         assert not bad, (groups, bad)
-        plan.set_tune(*batch_tunes[groups % len(batch_tunes)])
+        plan.set_tune(*fs.tune_table()[groups % len(fs.tune_table())])
 
 
 def test_batch_two_maps_and_camera_update(fs, orc, gpu_ctx, maps1024, maps256):
@@ -474,86 +471,3 @@ def test_l2_read_probe(gpu_ctx):
     """The roofline's L2 read bandwidth probe returns a finite positive rate."""
     gbs = gpu_ctx.measure_l2_read_gbs(16 << 20, 8)
     assert 100.0 < gbs < 1.0e6
-
-
-PIPE = (32, 1, 64, 3)
-
-
-@pytest.mark.parametrize("hf,cf", FILTERS)
-def test_row_pipeline_exact(fs, orc, gpu_ctx, maps256, hf, cf):
-    """The row pipeline (stage 3: rows of every sample, events per 64-depth
-    segment from the earlier segments' minima, colour and paint per event,
-    gap fill) on adversarial cameras (below and at the terrain), zero-colour
-    texels and both gap rules, degenerate and odd screen sizes, a
-    non-power-of-two map and the mode-B schedule."""
-    hm, cm = maps256
-    cm = cm.copy()
-    cm[::3, ::2] = 0
-    fmap = fs.Map(gpu_ctx, hm, cm)
-    hn = fs.gen_heights(3, 512, 0.6)[:300, :200].copy()
-    cn = fs.gen_colors(4, hn, 12)
-    fmap_n = fs.Map(gpu_ctx, hn, cn)
-    at = orc.lib().fso_height_bilinear(hm.ctypes.data, 256, 256, 64.5, 64.25)
-    cams = [fs.Camera(100.0, 100.0, 300.0, 0.0, 24.0, 200.0, 1.2, 0xFF9090E0),
-            fs.Camera(-37.0, -300.0, 120.0, 1.5707964, 30.0, 400.0, 1.2, 0xFF9090E0),
-            fs.Camera(64.5, 64.25, -10.0, 0.3, 24.0, 150.0, 1.2, 0xFF9090E0),
-            fs.Camera(64.5, 64.25, at, 0.3, 24.0, 150.0, 1.2, 0xFF9090E0),
-            fs.Camera(30.0, 40.0, 90.0, 2.0, 48.0, 0.5, 1.2, 0xFF9090E0)]
-    cams += fs.gen_cameras(171, hm, 2, above=(20, 90), distance=(400, 1500), screen_h=96)
-    gpu_ctx.force_tune(PIPE)
-    try:
-        for gap in (0, 1):
-            p = fs.default_params(height_filter=hf, color_filter=cf, gap_rule=gap)
-            for cam in cams:
-                for w, h in ((61, 47), (128, 96), (1, 1), (3, 300), (300, 3), (33, 65)):
-                    got = gpu_ctx.render(fmap, cam, w, h, params=p)
-                    ref = _oracle(orc, cam, p, hm, cm, w, h)
-                    assert count_diff(got, ref) == 0, (gap, w, h, cam.as_tuple())
-        p = fs.default_params(height_filter=hf, color_filter=cf)
-        for cam in fs.gen_cameras(9, hn, 2, above=(30, 60), distance=(300, 700), screen_h=90):
-            got = gpu_ctx.render(fmap_n, cam, 120, 90, params=p)
-            assert count_diff(got, _oracle(orc, cam, p, hn, cn, 120, 90)) == 0
-        pb = fs.default_params(invz_param1=0.005, invz_param2=1.0, magic_number=240.0,
-                               height_filter=hf, color_filter=cf, gap_rule=1, floor_n=0)
-        cam = fs.Camera(128.0, 200.0, 78.0, 0.0, 100.0, 800.0, 1.0, 0xFF9090E0)
-        got = gpu_ctx.render(fmap, cam, 800, 400, params=pb)
-        assert count_diff(got, _oracle(orc, cam, pb, hm, cm, 800, 400)) == 0
-        # the epilogue instantiation
-        for fx in (1, 2, 3):
-            pe = fs.default_params(height_filter=hf, color_filter=cf, effects=fx, shade=0.6,
-                                   fog_start=100.0, fog_end=900.0, fog_color=0xFF8090A0)
-            for cam in cams[4:]:
-                got = gpu_ctx.render(fmap, cam, 128, 96, params=pe)
-                assert count_diff(got, _oracle(orc, cam, pe, hm, cm, 128, 96)) == 0, fx
-    finally:
-        gpu_ctx.force_tune(None)
-
-
-def test_row_pipeline_1080p_walk_and_counters(fs, orc, gpu_ctx):
-    """1920x1080 frames over 4096^2 maps at D=3000 through the row pipeline,
-    frames back to back on one stream (the scratch is reused), against the
-    oracle; the work counters report every depth sample and the events."""
-    hm = fs.gen_heights(7, 4096, 0.55)
-    cm = fs.gen_colors(8, hm, 12)
-    fmap = fs.Map(gpu_ctx, hm, cm)
-    walk = fs.gen_walk(9, hm, 4, step=2.0, yaw=0.02, above=(30, 120), distance=3000.0,
-                       screen_h=1080)
-    p = fs.default_params()
-    torch = pytest.importorskip("torch")
-    outs = [torch.empty((1080, 1920), dtype=torch.int32, device="cuda") for _ in walk]
-    gpu_ctx.force_tune(PIPE)
-    try:
-        gpu_ctx.stats(True)
-        for c, o in zip(walk, outs):
-            gpu_ctx.render_device(fmap, c, 1920, 1080, o)
-        samples, events = gpu_ctx.stats(False)
-        assert samples == len(walk) * fs.num_depths(3000.0) * 1920
-        assert 0 < events < samples
-        for c, o in zip(walk, outs):
-            got = o.cpu().numpy().view(np.uint32)
-            assert count_diff(got, _oracle(orc, c, p, hm, cm, 1920, 1080)) == 0
-        # a shorter frame after a longer one: the scratch keeps its size
-        got = gpu_ctx.render(fmap, walk[0], 640, 480)
-        assert count_diff(got, _oracle(orc, walk[0], p, hm, cm, 640, 480)) == 0
-    finally:
-        gpu_ctx.force_tune(None)
