@@ -156,11 +156,16 @@ def by_resolution(views) -> dict:
 
 
 def check_sample(views) -> list[int]:
-    """Per resolution, the views with the largest and the smallest draw distance."""
+    """Per resolution, the views with the largest and the smallest draw
+    distance, plus the middle and the last view of that resolution when the
+    distances are all equal (at least two views per resolution)."""
     out = []
     for idxs in by_resolution(views).values():
         ds = [cam_field(views[i][0], "distance") for i in idxs]
-        for j in (int(np.argmax(ds)), int(np.argmin(ds))):
+        pick = [int(np.argmax(ds)), int(np.argmin(ds))]
+        if pick[0] == pick[1]:
+            pick += [len(idxs) // 2, len(idxs) - 1]
+        for j in pick:
             if idxs[j] not in out:
                 out.append(idxs[j])
     return sorted(out)
@@ -176,7 +181,7 @@ def oracle_diff(frames: dict, views, hm, cm, oparams) -> dict:
         bad += int(np.count_nonzero(ref != got))
     return {"frames_checked_vs_oracle": len(frames), "differing_pixels": bad,
             "checked_views": sorted(frames), "check": "per resolution the views with the "
-            "largest and smallest draw distance, after the timed region"}
+            "largest and smallest draw distance (at least two views), after the timed region"}
 
 
 class ClockSampler:
