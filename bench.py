@@ -490,6 +490,11 @@ def run_serve(args, rank: int, world: int):
                         "gpix_s": st["gpix_s"], "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
                         "mean_batch": st["mean_batch"], "batches": st["batches"],
                         "max_inflight": st["max_inflight"], "stall": stall,
+                        "loop_diagnostics": {
+                            "max_call_ms": st["max_call_ms"], "max_call_site": st["max_call_site"],
+                            "max_sleep_ms": st["max_sleep_ms"], "max_host_ms": st["max_host_ms"],
+                            "max_batch_gpu_ms": st["max_batch_gpu_ms"],
+                            "max_batch_gpu_at_s": st["max_batch_gpu_at_ns"] * 1e-9},
                         "peak_arena_gb": st["peak_arena_bytes"] / 2**30, "errors": st["errors"]})
     srv.close()
     if rank == 0:

@@ -75,10 +75,19 @@ class ServeStats(C.Structure):
                 ("p99_ms", C.c_double), ("mean_ms", C.c_double), ("max_ms", C.c_double),
                 ("requests", C.c_int64), ("pixels", C.c_int64), ("batches", C.c_int64),
                 ("mean_batch", C.c_double), ("peak_arena_bytes", C.c_int64),
-                ("max_inflight", C.c_int32), ("errors", C.c_int32)]
+                ("max_inflight", C.c_int32), ("errors", C.c_int32),
+                ("max_call_ms", C.c_double), ("max_call_site", C.c_int32),
+                ("reserved", C.c_int32), ("max_sleep_ms", C.c_double),
+                ("max_host_ms", C.c_double), ("max_batch_gpu_ms", C.c_double),
+                ("max_batch_gpu_at_ns", C.c_int64)]
+
+    SITES = {0: None, 1: "event query", 2: "copy in", 3: "counter reset", 4: "prologue launch",
+             5: "render launch", 6: "frame copy out", 7: "event record"}
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_}
+        d = {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+        d["max_call_site"] = self.SITES.get(d["max_call_site"], d["max_call_site"])
+        return d
 
 
 class View(C.Structure):

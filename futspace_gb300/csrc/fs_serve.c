@@ -103,7 +103,8 @@ static int arena_free(fs_arena *a, int64_t off, int64_t len) {
 
 typedef struct {
   cudaStream_t st;
-  cudaEvent_t ev;
+  cudaEvent_t ev0; /* recorded before the launch's first copy */
+  cudaEvent_t ev;  /* after its last operation */
   int32_t busy;
   int32_t nreq;
   int32_t *req;    /* request indices of the launch */
@@ -111,6 +112,7 @@ typedef struct {
                       [int64 items x max_items] */
   uint8_t *dev;    /* same layout on the device */
   int32_t *head_d;
+  int64_t launch_ns; /* when the current launch was enqueued (run clock) */
 } fs_slot;
 
 struct fs_server {
@@ -135,12 +137,23 @@ struct fs_server {
   float *zinvz;
   int8_t *sess_busy;
   fs_slot *slots;
+  int64_t iter_call_ns; /* CUDA call time within the current loop iteration */
 };
 
 static int64_t now_ns(void) {
   struct timespec t;
   clock_gettime(CLOCK_MONOTONIC, &t);
   return (int64_t)t.tv_sec * 1000000000LL + t.tv_nsec;
+}
+
+/* Diagnostics: a CUDA call of the loop took dt_ns at `site`. */
+static void note_call(fs_server *s, fs_serve_stats *st, int32_t site, int64_t dt_ns) {
+  s->iter_call_ns += dt_ns;
+  const double ms = (double)dt_ns * 1e-6;
+  if (ms > st->max_call_ms) {
+    st->max_call_ms = ms;
+    st->max_call_site = site;
+  }
 }
 
 void fs_server_free(fs_server *s) {
@@ -151,6 +164,7 @@ void fs_server_free(fs_server *s) {
       fs_slot *sl = &s->slots[i];
       if (sl->st) cudaStreamSynchronize(sl->st);
       if (sl->ev) cudaEventDestroy(sl->ev);
+      if (sl->ev0) cudaEventDestroy(sl->ev0);
       if (sl->st) cudaStreamDestroy(sl->st);
       cudaFreeHost(sl->pinned);
       cudaFree(sl->dev);
@@ -291,7 +305,7 @@ int fs_server_new(fs_ctx *ctx, fs_server **out, const fs_map *const *maps, int32
     fs_slot *sl = &s->slots[i];
     sl->req = (int32_t *)malloc(sizeof(int32_t) * (size_t)cfg->max_batch);
     if (!sl->req || cudaStreamCreateWithFlags(&sl->st, cudaStreamNonBlocking) ||
-        cudaEventCreateWithFlags(&sl->ev, cudaEventDisableTiming) ||
+        cudaEventCreate(&sl->ev) || cudaEventCreate(&sl->ev0) ||
         cudaMallocHost((void **)&sl->pinned, slot_bytes(s)) ||
         cudaMalloc((void **)&sl->dev, slot_bytes(s)) ||
         cudaMalloc((void **)&sl->head_d, sizeof(int32_t))) {
@@ -407,7 +421,10 @@ static int launch_batch(fs_server *s, fs_slot *sl, fs_request *reqs, fs_fifo *re
   for (int32_t i = 0; i < ni; i++) items[i] = scratch[i].item;
   sl->nreq = nb;
   const size_t used = items_offset(s) + 8 * (size_t)ni;
-  int e = cudaMemcpyAsync(sl->dev, sl->pinned, used, cudaMemcpyHostToDevice, sl->st);
+  int64_t tc = now_ns();
+  int e = cudaEventRecord(sl->ev0, sl->st);
+  if (!e) e = cudaMemcpyAsync(sl->dev, sl->pinned, used, cudaMemcpyHostToDevice, sl->st);
+  note_call(s, st, FS_SERVE_SITE_COPY_IN, now_ns() - tc);
   const FsView *packed_d = (const FsView *)sl->dev;
   const int32_t *ids_d = (const int32_t *)(sl->dev + sizeof(FsView) * (size_t)mb);
   const int64_t *items_d = (const int64_t *)(sl->dev + items_offset(s));
@@ -416,8 +433,12 @@ static int launch_batch(fs_server *s, fs_slot *sl, fs_request *reqs, fs_fifo *re
     if (packed[i].n > max_n) max_n = packed[i].n;
   /* the work counter is reset before the prologue kernel, so the render
    * kernel (a programmatic dependent launch) follows that kernel directly */
+  tc = now_ns();
   if (!e) e = cudaMemsetAsync(sl->head_d, 0, sizeof(int32_t), sl->st);
+  note_call(s, st, FS_SERVE_SITE_COUNTER_RESET, now_ns() - tc);
+  tc = now_ns();
   if (!e) e = fsk_serve_prepare(packed_d, ids_d, nb, max_n, s->sess_d, s->zline, s->zinvz, sl->st);
+  note_call(s, st, FS_SERVE_SITE_PROLOGUE, now_ns() - tc);
   if (!e) {
     FsLaunch L;
     memset(&L, 0, sizeof(L));
@@ -433,18 +454,26 @@ static int launch_batch(fs_server *s, fs_slot *sl, fs_request *reqs, fs_fifo *re
     const int32_t per_cta = fsk_items_per_cta(tune);
     const int32_t need = (ni + per_cta - 1) / per_cta;
     const int32_t grid = need < grid_max ? need : grid_max;
+    tc = now_ns();
     e = fsk_render_pdl(&L, tune, s->hf, s->cf, grid, sl->st);
+    note_call(s, st, FS_SERVE_SITE_RENDER, now_ns() - tc);
     ctx->launches += 2;
   }
   for (int32_t i = 0; i < nb && !e; i++) {
     const fs_request *r = &reqs[sl->req[i]];
-    if (r->host_out)
+    if (r->host_out) {
+      tc = now_ns();
       e = cudaMemcpyAsync(r->host_out, s->arena_base + frame_off[sl->req[i]],
                           (size_t)req_frame_bytes(r), cudaMemcpyDeviceToHost, sl->st);
+      note_call(s, st, FS_SERVE_SITE_COPY_OUT, now_ns() - tc);
+    }
   }
+  tc = now_ns();
   if (!e) e = cudaEventRecord(sl->ev, sl->st);
+  note_call(s, st, FS_SERVE_SITE_EVENT_RECORD, now_ns() - tc);
   if (e) return fs_cuda_fail(ctx, e, "serving launch");
   sl->busy = 1;
+  sl->launch_ns = now_ns() - t0;
   st->batches++;
   st->mean_batch += nb;
   return FS_OK;
@@ -499,7 +528,10 @@ int fs_server_run(fs_server *s, fs_request *reqs, int32_t n, int32_t realtime,
   const int64_t t0 = now_ns();
   while (completed < n && !rc) {
     int progress = 0;
-    const int64_t now = now_ns() - t0;
+    const int64_t t_iter = now_ns();
+    int64_t slept = 0;
+    s->iter_call_ns = 0;
+    const int64_t now = t_iter - t0;
     /* release arrivals */
     while (next < n && (!realtime || reqs[order[next]].arrival_ns <= now)) {
       fifo_push(&pending, order[next++]);
@@ -539,13 +571,21 @@ int fs_server_run(fs_server *s, fs_request *reqs, int32_t n, int32_t realtime,
     for (int i = 0; i < s->cfg.slots; i++) {
       fs_slot *sl = &s->slots[i];
       if (!sl->busy) continue;
+      const int64_t tq = now_ns();
       const cudaError_t q = cudaEventQuery(sl->ev);
+      note_call(s, &st, FS_SERVE_SITE_EVENT_QUERY, now_ns() - tq);
       if (q == cudaErrorNotReady) continue;
       if (q != cudaSuccess) {
         rc = fs_cuda_fail(ctx, q, "serving batch");
         break;
       }
       const int64_t done = now_ns() - t0;
+      float gpu_ms = 0.0f;
+      if (cudaEventElapsedTime(&gpu_ms, sl->ev0, sl->ev) == cudaSuccess &&
+          (double)gpu_ms > st.max_batch_gpu_ms) {
+        st.max_batch_gpu_ms = (double)gpu_ms;
+        st.max_batch_gpu_at_ns = sl->launch_ns;
+      }
       for (int32_t k = 0; k < sl->nreq; k++) {
         const int32_t ri = sl->req[k];
         fs_request *r = &reqs[ri];
@@ -573,8 +613,13 @@ int fs_server_run(fs_server *s, fs_request *reqs, int32_t n, int32_t realtime,
       /* idle until the next arrival or a completion: short sleeps keep the
        * host clock pacing accurate to a few microseconds */
       struct timespec ts = {0, 2000};
+      const int64_t ts0 = now_ns();
       nanosleep(&ts, NULL);
+      slept = now_ns() - ts0;
+      if ((double)slept * 1e-6 > st.max_sleep_ms) st.max_sleep_ms = (double)slept * 1e-6;
     }
+    const double host_ms = (double)(now_ns() - t_iter - slept - s->iter_call_ns) * 1e-6;
+    if (host_ms > st.max_host_ms) st.max_host_ms = host_ms;
   }
   const int64_t t_end = now_ns() - t0;
   /* drain anything still in flight after an error */

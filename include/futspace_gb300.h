@@ -295,7 +295,28 @@ typedef struct {
   int64_t peak_arena_bytes;
   int32_t max_inflight;
   int32_t errors;
+  /* where the slowest moments of the run went (diagnostics): the longest
+   * single CUDA runtime call of the loop and its FS_SERVE_SITE_*, the longest
+   * idle sleep (2 us requested), the longest loop iteration without its calls
+   * and sleeps (host time), and the longest launch on the GPU (from the event
+   * before its first copy to its completion event) with its launch time */
+  double max_call_ms;
+  int32_t max_call_site;
+  int32_t reserved;
+  double max_sleep_ms;
+  double max_host_ms;
+  double max_batch_gpu_ms;
+  int64_t max_batch_gpu_at_ns;
 } fs_serve_stats;
+enum {
+  FS_SERVE_SITE_EVENT_QUERY = 1,
+  FS_SERVE_SITE_COPY_IN = 2,
+  FS_SERVE_SITE_COUNTER_RESET = 3,
+  FS_SERVE_SITE_PROLOGUE = 4,
+  FS_SERVE_SITE_RENDER = 5,
+  FS_SERVE_SITE_COPY_OUT = 6,
+  FS_SERVE_SITE_EVENT_RECORD = 7
+};
 
 typedef struct fs_server fs_server;
 int fs_server_new(fs_ctx *ctx, fs_server **out, const fs_map *const *maps, int32_t nmaps,
