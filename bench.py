@@ -420,6 +420,25 @@ def run_reference(args, rank: int, world: int):
     print(json.dumps(line), flush=True)
 
 
+def _read(path: str):
+    try:
+        return Path(path).read_text().strip()
+    except OSError:
+        return None
+
+
+def cgroup_cpu_stat() -> dict:
+    """The process's cgroup CPU counters (cgroup v2 cpu.stat), {} if absent."""
+    out = {}
+    try:
+        for line in Path("/sys/fs/cgroup/cpu.stat").read_text().splitlines():
+            k, v = line.split()
+            out[k] = int(v)
+    except (OSError, ValueError):
+        pass
+    return out
+
+
 def run_serve(args, rank: int, world: int):
     """Serving: Poisson arrivals from 64 sessions (seeded camera walks), request
     sizes mixed as the batch512 workload, 4096^2 and 8192^2 map sets resident,
@@ -468,7 +487,9 @@ def run_serve(args, rank: int, world: int):
             if i in sample:
                 bufs[i] = fs.PinnedBuffer((h, w))
                 r.host_out = bufs[i].ptr
+        cg0 = cgroup_cpu_stat()
         st = srv.run(reqs, realtime=True)
+        cg1 = cgroup_cpu_stat()
         # where the slowest requests arrived (a stall shows as one window)
         lat = np.array([(reqs[i].done_ns - reqs[i].arrival_ns) * 1e-6 for i in range(n)])
         arr_s = arrivals * 1e-9
@@ -494,7 +515,12 @@ def run_serve(args, rank: int, world: int):
                             "max_call_ms": st["max_call_ms"], "max_call_site": st["max_call_site"],
                             "max_sleep_ms": st["max_sleep_ms"], "max_host_ms": st["max_host_ms"],
                             "max_batch_gpu_ms": st["max_batch_gpu_ms"],
-                            "max_batch_gpu_at_s": st["max_batch_gpu_at_ns"] * 1e-9},
+                            "max_batch_gpu_at_s": st["max_batch_gpu_at_ns"] * 1e-9,
+                            "max_host_at_s": st["max_host_at_ns"] * 1e-9,
+                            "involuntary_switches": st["involuntary_switches"],
+                            "voluntary_switches": st["voluntary_switches"],
+                            "cgroup_throttled": {k: cg1[k] - cg0.get(k, 0) for k in cg1
+                                                 if k.startswith(("nr_throttled", "throttled"))}},
                         "peak_arena_gb": st["peak_arena_bytes"] / 2**30, "errors": st["errors"]})
     srv.close()
     if rank == 0:
@@ -510,6 +536,7 @@ def run_serve(args, rank: int, world: int):
                        "seconds_per_rate": args.serve_seconds},
             "serving": results,
             "frames_checked_vs_oracle": checked, "differing_pixels": bad,
+            "host": {"cpus": os.cpu_count(), "cgroup_cpu_max": _read("/sys/fs/cgroup/cpu.max")},
         }
         print(json.dumps(line), flush=True)
 
@@ -719,6 +746,29 @@ def plan_leg(fs, ctx, args, name: str, rank: int, world: int, local: int, steps:
         frames[i] = flat[o:o + w * h].reshape(h, w).copy()
     parity = oracle_diff(frames, views, hm, cm, oracle_params(name))
 
+    # the kernel forms on this plan, one configuration each (the autotuner
+    # times every compiled configuration; these are the best-known of each
+    # form): direct painting, the shared-memory stage with TMA row stores, the
+    # cooperative tile
+    forms = None
+    if headline and not args.no_forms and world == 1:
+        forms = {}
+        for label, t in (("direct painting (64,2,4,0)", (64, 2, 4, 0)),
+                         ("staged, TMA row stores (8,32,2,1)", (8, 32, 2, 1)),
+                         ("cooperative tile (8,64,8,2)", (8, 64, 8, 2))):
+            try:
+                plan.set_tune(*t)
+            except fs.FsError as e:
+                forms[label] = f"unsupported: {e}"
+                continue
+            plan.run()
+            ks: list[float] = []
+            timed(plan.run, 5, ks)
+            forms[label] = {"kernel_ms": float(np.median(ks))}
+        plan.set_tune(*tune[:4])
+        plan.run()
+        ctx.sync()
+
     t_plain = []
     if headline and not args.no_plain:
         # the per-frame loop runs each resolution with its own autotuned configuration
@@ -797,6 +847,7 @@ def plan_leg(fs, ctx, args, name: str, rank: int, world: int, local: int, steps:
             "p99_ms": float(np.percentile(t_plain, 99)),
             "launches_per_step": 2 * len(views)},
         "batched_over_plain": None if not t_plain else float(np.mean(t_plain)) / ms,
+        "kernel_forms": forms,
         "frames_per_s": len(views) * world / ms_max * 1e3,
         "work": {"depth_samples": samples, "full_depth_samples": full_s,
                  "events_coloured": events},
@@ -836,6 +887,8 @@ def main():
     ap.add_argument("--e2e-groups", type=int, default=8,
                     help="view groups of the pipelined render + download in the e2e timing")
     ap.add_argument("--no-plain", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip timing the three kernel forms on the main plan")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the shorter workloads run beside the default batch512 line")
     ap.add_argument("--extra-steps", type=int, default=10)

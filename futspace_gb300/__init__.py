@@ -79,7 +79,8 @@ class ServeStats(C.Structure):
                 ("max_call_ms", C.c_double), ("max_call_site", C.c_int32),
                 ("reserved", C.c_int32), ("max_sleep_ms", C.c_double),
                 ("max_host_ms", C.c_double), ("max_batch_gpu_ms", C.c_double),
-                ("max_batch_gpu_at_ns", C.c_int64)]
+                ("max_batch_gpu_at_ns", C.c_int64), ("max_host_at_ns", C.c_int64),
+                ("involuntary_switches", C.c_int64), ("voluntary_switches", C.c_int64)]
 
     SITES = {0: None, 1: "event query", 2: "copy in", 3: "counter reset", 4: "prologue launch",
              5: "render launch", 6: "frame copy out", 7: "event record"}

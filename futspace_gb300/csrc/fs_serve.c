@@ -23,6 +23,7 @@
 #endif
 #include <stdlib.h>
 #include <string.h>
+#include <sys/resource.h>
 #include <time.h>
 
 #include "fs_internal.h"
@@ -525,6 +526,9 @@ int fs_server_run(fs_server *s, fs_request *reqs, int32_t n, int32_t realtime,
   fs_fifo pending = {pq, 0, 0, n ? n : 1}, ready = {rq, 0, 0, n ? n : 1};
   int32_t next = 0, completed = 0, batch_id = 0, inflight = 0;
   int rc = FS_OK;
+  struct rusage ru0;
+  memset(&ru0, 0, sizeof(ru0));
+  getrusage(RUSAGE_THREAD, &ru0);
   const int64_t t0 = now_ns();
   while (completed < n && !rc) {
     int progress = 0;
@@ -619,7 +623,17 @@ int fs_server_run(fs_server *s, fs_request *reqs, int32_t n, int32_t realtime,
       if ((double)slept * 1e-6 > st.max_sleep_ms) st.max_sleep_ms = (double)slept * 1e-6;
     }
     const double host_ms = (double)(now_ns() - t_iter - slept - s->iter_call_ns) * 1e-6;
-    if (host_ms > st.max_host_ms) st.max_host_ms = host_ms;
+    if (host_ms > st.max_host_ms) {
+      st.max_host_ms = host_ms;
+      st.max_host_at_ns = now;
+    }
+  }
+  {
+    struct rusage ru1;
+    memset(&ru1, 0, sizeof(ru1));
+    getrusage(RUSAGE_THREAD, &ru1);
+    st.involuntary_switches = (int64_t)(ru1.ru_nivcsw - ru0.ru_nivcsw);
+    st.voluntary_switches = (int64_t)(ru1.ru_nvcsw - ru0.ru_nvcsw);
   }
   const int64_t t_end = now_ns() - t0;
   /* drain anything still in flight after an error */

@@ -307,6 +307,9 @@ typedef struct {
   double max_host_ms;
   double max_batch_gpu_ms;
   int64_t max_batch_gpu_at_ns;
+  int64_t max_host_at_ns;      /* when the longest host-only iteration started */
+  int64_t involuntary_switches; /* of the loop's thread during the run (getrusage) */
+  int64_t voluntary_switches;
 } fs_serve_stats;
 enum {
   FS_SERVE_SITE_EVENT_QUERY = 1,
