@@ -746,29 +746,6 @@ def plan_leg(fs, ctx, args, name: str, rank: int, world: int, local: int, steps:
         frames[i] = flat[o:o + w * h].reshape(h, w).copy()
     parity = oracle_diff(frames, views, hm, cm, oracle_params(name))
 
-    # the kernel forms on this plan, one configuration each (the autotuner
-    # times every compiled configuration; these are the best-known of each
-    # form): direct painting, the shared-memory stage with TMA row stores, the
-    # cooperative tile
-    forms = None
-    if headline and not args.no_forms and world == 1:
-        forms = {}
-        for label, t in (("direct painting (64,2,4,0)", (64, 2, 4, 0)),
-                         ("staged, TMA row stores (8,32,2,1)", (8, 32, 2, 1)),
-                         ("cooperative tile (8,64,8,2)", (8, 64, 8, 2))):
-            try:
-                plan.set_tune(*t)
-            except fs.FsError as e:
-                forms[label] = f"unsupported: {e}"
-                continue
-            plan.run()
-            ks: list[float] = []
-            timed(plan.run, 5, ks)
-            forms[label] = {"kernel_ms": float(np.median(ks))}
-        plan.set_tune(*tune[:4])
-        plan.run()
-        ctx.sync()
-
     t_plain = []
     if headline and not args.no_plain:
         # the per-frame loop runs each resolution with its own autotuned configuration
@@ -803,6 +780,29 @@ def plan_leg(fs, ctx, args, name: str, rank: int, world: int, local: int, steps:
                "h2d_bytes_per_step": 96 * len(views),  # one 96-byte view record per camera
                "d2h_bytes_per_step": 4 * plan.total_pixels,
                "ms_per_step": e2e_ms, "groups": args.e2e_groups}
+
+    # the kernel forms on this plan, one configuration each (the autotuner
+    # times every compiled configuration; these are the best-known of each
+    # form): direct painting, the shared-memory stage with TMA row stores, the
+    # cooperative tile
+    forms = None
+    if headline and not args.no_forms and world == 1:
+        forms = {}
+        for label, t in (("direct painting (64,2,4,0)", (64, 2, 4, 0)),
+                         ("staged, TMA row stores (8,32,2,1)", (8, 32, 2, 1)),
+                         ("cooperative tile (8,64,8,2)", (8, 64, 8, 2))):
+            try:
+                plan.set_tune(*t)
+            except fs.FsError as e:
+                forms[label] = f"unsupported: {e}"
+                continue
+            plan.run()
+            ks: list[float] = []
+            timed(plan.run, 5, ks)
+            forms[label] = {"kernel_ms": float(np.median(ks))}
+        plan.set_tune(*tune[:4])
+        plan.run()
+        ctx.sync()
 
     ms = float(np.mean(t_batch))
     # replicas: every rank renders its own views; sum pixels, slowest rank's time

@@ -1027,9 +1027,15 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
       /* the warp's depths [ka, kz] over its TW columns */
       const int jw = warp * (32 / TW);
       const int ka = kb + jw * U, kz = min(kb + (jw + 32 / TW) * U, n) - 1;
-      bool skip = ka > kz || __all_sync(FS_FULL_MASK, mstart == 0);
+      /* rest: every later block of the warp's depths is skipped too. The
+       * column minima only decrease, so a bound not above today's largest
+       * minimum stays so; when every warp agrees, the tile ends after this
+       * block (its trailing blocks would find no event). */
+      bool rest = ka > kz || __all_sync(FS_FULL_MASK, mstart == 0);
+      bool skip = rest;
       if (!skip && M.pyr) {
         const float cf = (float)c0, cl = (float)max(c0, min(c0 + TW, W) - 1);
+        const int mmax = (int)__reduce_max_sync(FS_FULL_MASK, (unsigned)mstart);
         int b;
         if (param_view && bi == 0) {
           /* a plain call's block 0 marches before the depth-table kernel has
@@ -1047,8 +1053,11 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
               bbound = chunk_row_bound(M, zl, zi, cam_h, horizon, H, cf, cl, kal, kzl);
           }
           b = __shfl_sync(FS_FULL_MASK, bbound, bi - bbase);
+          /* lane l bounds block bbase + l; the window must reach the last block */
+          rest = (n - 1) / NB <= bbase + 31 &&
+                 __all_sync(FS_FULL_MASK, bbase + lane <= bi || bbound >= mmax);
         }
-        skip = b >= (int)__reduce_max_sync(FS_FULL_MASK, (unsigned)mstart);
+        skip = b >= mmax;
       }
       if (!skip && mstart > 0) {
         auto rows = [&](auto p2tag) {
@@ -1097,7 +1106,7 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
           iznext[q] = __ldg(zi + kb + NB + e);
         }
       }
-      __syncthreads();
+      const bool tile_rest = __syncthreads_and(rest ? 1 : 0) != 0;
 
       /* Y: the minimum before each sample, the block's events (B), and the
        * next block's depth-table entries */
@@ -1163,9 +1172,10 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
       if (tid == 0) scal[par ^ 1] = 0; /* the previous block's list is coloured */
       __syncthreads();
 
-      /* the last block, or every column at row 0: colour it and finish */
+      /* the last block, every column at row 0, or no event possible in any
+       * later block: colour this block and finish */
       bool done = !more;
-      if (more) done = scal[3] != 0;
+      if (more) done = scal[3] != 0 || tile_rest;
       if (done) {
         colour_events(par, kb);
         break;
