@@ -672,7 +672,8 @@ int fs_render_view(fs_ctx *ctx, const FsMapDev *map, FsView *v, const FsTune *tu
   L->view0.map = 0;
   L->zline = zline;
   L->zinvz = zinvz;
-  L->stats = ctx->stats_dev;
+  /* the work counters cost instructions per depth chunk: only when collected */
+  L->stats = ctx->collect_stats ? ctx->stats_dev : NULL;
   L->nitems = ntiles * v->nseg;
   L->stride_max = stride;
   /* the timer brackets every kernel of the call; an event between two of them

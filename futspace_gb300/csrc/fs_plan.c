@@ -77,7 +77,8 @@ static void plan_fill_launch(fs_plan *p, FsLaunch *L) {
   L->head = p->head_d;
   L->nitems = p->nitems;
   L->stride_max = p->stride_max;
-  L->stats = p->ctx->stats_dev;
+  /* the work counters cost instructions per depth chunk: only when collected */
+  L->stats = p->ctx->collect_stats ? p->ctx->stats_dev : NULL;
 }
 
 /* The segment-minimum pass over every split view (none when nothing is split). */
@@ -142,6 +143,7 @@ static int plan_build(fs_plan *p) {
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
   plan_release_graph(p);
+  p->built_stats = ctx->collect_stats;
   int32_t occ = 0;
   int e = fsk_render_max_ctas_per_sm(&p->tune, p->hf, p->cf, p->stride_max, &occ);
   if (e) return fs_cuda_fail(ctx, e, "occupancy query");
@@ -401,6 +403,12 @@ int fs_plan_run(fs_plan *p) {
   fs_ctx *ctx = p->ctx;
   if (!p->graph_ok) return fs_fail(ctx, FS_ERR_STATE, "plan has no graph");
   cudaSetDevice(ctx->device);
+  /* the graph holds the launch parameters: rebuild it when the context
+   * started or stopped collecting work counters since it was captured */
+  if (p->built_stats != ctx->collect_stats) {
+    const int rc = plan_build(p);
+    if (rc) return rc;
+  }
   int e = cudaGraphLaunch(p->exec, ctx->stream);
   if (e) return fs_cuda_fail(ctx, e, "cudaGraphLaunch");
   /* depth tables + render, plus the segment-minimum and gap-fill passes */

@@ -94,6 +94,7 @@ struct fs_plan {
   cudaGraph_t graph;
   cudaGraphExec_t exec;
   int32_t graph_ok;
+  int32_t built_stats; /* ctx->collect_stats when the graph was captured */
   cudaEvent_t ev_render[2]; /* recorded around the render kernel inside the graph */
   int64_t *items_h;          /* the items in launch order (host copy) */
   /* pipelined render + download (fs_plan_run_download): views split into

@@ -402,6 +402,17 @@ __device__ __forceinline__ void render_strip(const FsLaunch &P, const FsView *Vp
     __syncwarp();
   };
 
+  /* A chunk none of whose rows lies above its column's minimum holds no
+   * event and leaves the minimum as it is (an event needs a row below the
+   * running minimum, which never exceeds m within the chunk): its per-depth
+   * scans are skipped. Warp-uniform. */
+  auto no_event = [&](const int(&r)[U]) -> bool {
+    int rmin = r[0];
+#pragma unroll
+    for (int u = 1; u < U; u++) rmin = min(rmin, r[u]);
+    return !__any_sync(FS_FULL_MASK, rmin < m);
+  };
+
   /* rows of one chunk of depth samples, then its events into the ring */
   auto march_chunk = [&](auto p2tag, int k0) {
     int r[U];
@@ -414,6 +425,7 @@ __device__ __forceinline__ void render_strip(const FsLaunch &P, const FsView *Vp
         const int rr = sample_row(p2tag, k);
         r[u] = k < k_end ? rr : H;
       }
+      if (no_event(r)) return;
 #pragma unroll
       for (int u = 0; u < U; u++) {
         const bool ev = r[u] < m;
@@ -450,6 +462,7 @@ __device__ __forceinline__ void render_strip(const FsLaunch &P, const FsView *Vp
         const int rr = sample_row(p2tag, k);
         r[u] = k < k_end ? rr : H;
       }
+      if (no_event(r)) return;
 #pragma unroll
       for (int u = 0; u < U; u++) {
         int incl = r[u];

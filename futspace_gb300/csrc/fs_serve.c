@@ -449,7 +449,7 @@ static int launch_batch(fs_server *s, fs_slot *sl, fs_request *reqs, fs_fifo *re
     L.zline = s->zline;
     L.zinvz = s->zinvz;
     L.head = sl->head_d;
-    L.stats = ctx->stats_dev;
+    L.stats = ctx->collect_stats ? ctx->stats_dev : NULL;
     L.nitems = ni;
     L.stride_max = stride;
     const int32_t per_cta = fsk_items_per_cta(tune);

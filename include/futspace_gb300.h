@@ -241,8 +241,10 @@ int fs_tune_count(void);
 int fs_tune_get(int i, int32_t out5[5]);
 
 /* Work counters of the render kernel: when enabled, every following launch adds
- * the depth samples it evaluated and the occlusion events it coloured. Reading
- * (out2 != NULL) waits for the stream and resets the counters. */
+ * the depth samples it evaluated and the occlusion events it coloured (when
+ * disabled, the kernels skip the counting). Reading (out2 != NULL) waits for
+ * the stream and resets the counters. A plan recaptures its graph at its next
+ * run after the setting changes. */
 int fs_ctx_stats(fs_ctx *ctx, int32_t enable, uint64_t out2[2]);
 
 /* Roofline denominator: L2 read bandwidth in GB/s, from one kernel reading a
