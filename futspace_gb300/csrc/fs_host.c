@@ -581,6 +581,19 @@ FsTune fs_tune_for_mode(FsTune t, int32_t view_flags) {
   return t;
 }
 
+int fs_coop_depths_ok(const FsTune *t, int32_t max_n) {
+  return t->stage != 2 || max_n <= FS_COOP_MAX_DEPTHS;
+}
+
+/* The first table entry other than the cooperative tile that fits. */
+FsTune fs_default_tune_without_coop(fs_ctx *ctx, int32_t stride_max) {
+  for (int i = 0; i < fs_tune_count(); i++)
+    if (k_tune_order[i].stage != 2 && fs_tune_fits(ctx, &k_tune_order[i], stride_max))
+      return k_tune_order[i];
+  FsTune none = {0, 0, 0, 0, 0};
+  return none;
+}
+
 /* Default choice when the tuning cache has no entry: the first table entry
  * whose shared-memory stage fits. */
 FsTune fs_default_tune(fs_ctx *ctx, int32_t stride_max) {
@@ -633,6 +646,10 @@ int fs_render_view(fs_ctx *ctx, const FsMapDev *map, FsView *v, const FsTune *tu
   else if (!fs_tune_lookup(ctx, v->W, v->H, map->MH, map->MW, v->flags, &t))
     t = fs_default_tune(ctx, stride);
   t = fs_tune_for_mode(t, v->flags);
+  if (t.stage == 2 && v->n > FS_COOP_MAX_DEPTHS) {
+    /* more depths than the cooperative tile's event entries hold */
+    t = fs_tune_for_mode(fs_default_tune_without_coop(ctx, stride), v->flags);
+  }
   if (!t.tw || !fs_tune_fits(ctx, &t, stride))
     return fs_fail(ctx, FS_ERR_ARG, "no kernel configuration fits screen height %d", v->H);
   const int32_t hf = (v->flags & FSV_HEIGHT_BILINEAR) != 0;

@@ -26,6 +26,11 @@ extern "C" {
  * render kernel loads whole chunks of depths (at most FS_ZPAD) without a bound
  * check and discards the rows of depths past n. The entries are zeros. */
 #define FS_ZPAD 64
+/* Limits of the cooperative tile's 32-bit event entries (pack_coop_event in
+ * fs_render.cuh): depths per view, screen rows. Views beyond them render with
+ * the other kernel forms. */
+#define FS_COOP_MAX_DEPTHS (1 << 17)
+#define FS_COOP_MAX_ROWS 4095
 /* Maps bound to one launch. */
 #define FS_MAX_MAPS 4
 /* Levels of the height max pyramid (2^16 texels per side). */

@@ -203,9 +203,12 @@ extern "C" int fsk_tune_supported(const FsTune *t) {
 }
 
 extern "C" size_t fsk_render_smem(const FsTune *t, int32_t stride_max) {
+  /* the cooperative tile: fixed part, stage and event list; taller frames
+   * than its event entries hold never fit */
+  if (t->stage == 2 && stride_max > FS_COOP_MAX_ROWS) return (size_t)1 << 40;
 #define FS_COOP_SMEM(TW_, TPC_, U_)                                  \
   if (t->stage == 2 && t->tw == TW_ && t->lc == TPC_ && t->u == U_) \
-    return CoopShape<TW_, TPC_, U_>::fixed_bytes + CoopShape<TW_, TPC_, U_>::stage_bytes(stride_max);
+    return CoopShape<TW_, TPC_, U_>::fixed_bytes + CoopShape<TW_, TPC_, U_>::tile_bytes(stride_max);
   FS_COOP_LIST(FS_COOP_SMEM)
 #undef FS_COOP_SMEM
   /* must match RenderShape<...>::fixed_bytes + stage */

@@ -135,6 +135,14 @@ static int plan_enqueue(fs_plan *p) {
 
 /* (Re)builds everything that depends on the tuning: tensor maps (box width),
  * work items (tile width), grid size and the captured graph. */
+/* The largest depth count of the plan's views (their capacity). */
+int32_t fs_plan_max_depths(const fs_plan *p) {
+  int32_t m = 0;
+  for (int v = 0; v < p->nviews; v++)
+    if (p->ncap[v] > m) m = p->ncap[v];
+  return m;
+}
+
 static int plan_build(fs_plan *p) {
   fs_ctx *ctx = p->ctx;
   const int32_t tw = p->tune.tw;
@@ -353,7 +361,8 @@ int fs_plan_new(fs_ctx *ctx, fs_plan **out, const fs_map *const *maps, int32_t n
   snprintf(key, sizeof(key), "batch:%016llx:map%dx%d:f%d", (unsigned long long)batch_signature(p),
            p->maps[0].MH, p->maps[0].MW, p->hf | (p->cf << 1));
   FsTune t;
-  if (!fs_tune_lookup_key(ctx, key, &t) || !fs_tune_fits(ctx, &t, p->stride_max))
+  if (!fs_tune_lookup_key(ctx, key, &t) || !fs_tune_fits(ctx, &t, p->stride_max) ||
+      !fs_coop_depths_ok(&t, fs_plan_max_depths(p)))
     t = fs_default_batch_tune(ctx, p->stride_max);
   if (!t.tw) {
     fs_plan_free(p);
@@ -578,6 +587,9 @@ int fs_plan_set_tune(fs_plan *p, const int32_t tune5[5]) {
   if (!fs_tune_fits(p->ctx, &t, p->stride_max))
     return fs_fail(p->ctx, FS_ERR_ARG, "tuning (%d,%d,%d,%d) unsupported or too large", t.tw,
                    t.lc, t.u, t.stage);
+  if (!fs_coop_depths_ok(&t, fs_plan_max_depths(p)))
+    return fs_fail(p->ctx, FS_ERR_ARG, "the cooperative tile holds at most %d depths per view",
+                   FS_COOP_MAX_DEPTHS);
   p->tune = t;
   return plan_build(p);
 }

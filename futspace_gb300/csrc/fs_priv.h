@@ -129,6 +129,11 @@ void fs_set_segments(FsView *v, int32_t nseg, int32_t chunk);
 int fs_tune_fits(fs_ctx *ctx, const FsTune *t, int32_t stride_max);
 FsTune fs_tune_for_mode(FsTune t, int32_t view_flags);
 FsTune fs_default_tune(fs_ctx *ctx, int32_t stride_max);
+FsTune fs_default_tune_without_coop(fs_ctx *ctx, int32_t stride_max);
+/* 1 unless t is the cooperative tile and a view has more depths than its
+ * event entries hold */
+int fs_coop_depths_ok(const FsTune *t, int32_t max_n);
+int32_t fs_plan_max_depths(const fs_plan *p);
 int fs_tune_count(void);
 int fs_tune_get(int i, int32_t out5[5]);
 

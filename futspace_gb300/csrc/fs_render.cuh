@@ -822,44 +822,47 @@ __global__ void __launch_bounds__(TW *LC, 1024 / (TW * LC)) segmin_kernel(
  *  B. the running minimum before each sample comes from a min-scan over the
  *     column's threads: the thread's own U rows, a warp scan (__shfl_up_sync
  *     in steps of TW lanes) and the warp totals in shared memory; events (row
- *     below that minimum) go to the block's list;
- *  C. all warps colour the listed events and write each colour at its event's
- *     row of the stage, which starts the tile filled with the gap value: this
- *     is the reference's scatter (fut/voxel_renderer.fut:244); its forward fill
- *     (:246) runs once over the finished tile.
- * Phases C of block b-1 and A of block b run together, and block b+1's
- * depth-table entries load into registers at the end of A and go to shared
- * memory during B (two buffers each), so a block costs two barriers and its
- * colour gathers overlap the next block's height gathers. A plain call (the
- * view is a kernel parameter) computes block 0's entries in the CTA and
- * marches it while the depth-table kernel finishes. (Copying the next
- * block's entries with cp.async while block b marches, into a third buffer,
- * made the 1920x1080 frame 20 % slower.) The column chain is one block per
- * step instead of one chunk, so a single frame with few columns keeps every
- * SM busy. After the last block (or once every column's minimum is row 0)
- * the tile gets the forward fill and sky, spread over all threads of the
- * tile. The stage is row-major, so every 32-row box of the tile goes to the
- * frame straight from it with TMA, all boxes back to back. */
+ *     below that minimum) go to the tile's event list in shared memory.
+ * Block b+1's depth-table entries load into registers at the end of A and go
+ * to shared memory during B (two buffers), so a block costs two barriers. A
+ * plain call (the view is a kernel parameter) computes block 0's entries in
+ * the CTA and marches it while the depth-table kernel finishes. (Copying the
+ * next block's entries with cp.async while block b marches, into a third
+ * buffer, made the 1920x1080 frame 20 % slower.) The column chain is one
+ * block per step instead of one chunk, so a single frame with few columns
+ * keeps every SM busy.
+ * Colouring does not feed the march (the running minima come from rows
+ * alone), so it stays off the chain of blocks: after the last block (or once
+ * every column's minimum is row 0, or no later block can hold an event) every
+ * thread colours the listed events and writes each colour at its event's row
+ * of the stage, which starts the tile filled with the gap value: this is the
+ * reference's scatter (fut/voxel_renderer.fut:244). (Colouring block b-1's
+ * events beside block b's rows put the near blocks' many events on the chain:
+ * 36.1 against 29.3 us for the 1920x1080 frame.) Then the forward fill (:246)
+ * and sky, spread over all threads of the tile. The stage is row-major, so
+ * every 32-row box of the tile goes to the frame straight from it with TMA,
+ * all boxes back to back. */
 template <int TW, int TPC, int U>
 struct CoopShape {
   static constexpr int NT = TW * TPC;
   static constexpr int NW = NT / 32;
   static constexpr int NB = TPC * U;   /* depths per block */
-  static constexpr int ECAP = TW * NB; /* events per block: at most one per sample */
   static constexpr size_t lut_bytes = 256 * 4;
   static constexpr size_t zl_bytes = 2ull * NB * 16; /* two blocks' entries */
   static constexpr size_t zi_bytes = 2ull * NB * 4;
-  static constexpr size_t ev_bytes = 2ull * ECAP * 4; /* two blocks' event lists */
-  /* warp totals [NW][TW], block-start minima [2][TW], event counts [2], item */
+  /* warp totals [NW][TW], block-start minima [2][TW], event count, item */
   static constexpr size_t misc_bytes = ((size_t)NW * TW + 2 * TW + 4) * 4;
   /* the stage starts on a 128-byte boundary, as do its boxes (TMA sources) */
   static constexpr size_t fixed_bytes =
-      (lut_bytes + zl_bytes + zi_bytes + ev_bytes + misc_bytes + 127) / 128 * 128;
+      (lut_bytes + zl_bytes + zi_bytes + misc_bytes + 127) / 128 * 128;
   static constexpr int min_blocks = NT >= 1024 ? 1 : 1024 / NT;
   /* the stage: row-major [H rounded up to whole boxes][TW] */
   static __host__ __device__ constexpr size_t stage_bytes(int H) {
     return (size_t)TW * (size_t)((H + kBoxRows - 1) / kBoxRows * kBoxRows) * 4;
   }
+  /* the stage, then the tile's event list: every event lowers its column's
+   * minimum row, so a tile holds at most TW * H of them (4 bytes each) */
+  static __host__ __device__ constexpr size_t tile_bytes(int H) { return 2 * stage_bytes(H); }
 };
 
 /* Writes a row-major [rows][TW] stage to the frame: every 32-row box straight
@@ -891,33 +894,34 @@ __device__ __forceinline__ void store_rows(const FsLaunch &P, const FsView *Vp, 
   __syncthreads();
 }
 
-/* Event list entry of the cooperative tile: depth within the block (11 bits),
- * tile column (5), row (16). */
-__device__ __forceinline__ uint32_t pack_coop_event(int kl, int c, int row) {
-  return ((uint32_t)kl << 21) | ((uint32_t)c << 16) | (uint32_t)row;
+/* Event list entry of the cooperative tile: depth (17 bits), tile column
+ * (3), row (12). The host keeps views with more depths, taller frames or
+ * wider tiles off this kernel (FS_COOP_MAX_DEPTHS, FS_COOP_MAX_ROWS). */
+__device__ __forceinline__ uint32_t pack_coop_event(int k, int c, int row) {
+  return ((uint32_t)k << 15) | ((uint32_t)c << 12) | (uint32_t)row;
 }
 
 template <int TW, int TPC, int U, int HF, int CF, int FX>
 __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
     coop_kernel(const __grid_constant__ FsLaunch P) {
   using S = CoopShape<TW, TPC, U>;
-  constexpr int NT = S::NT, NW = S::NW, NB = S::NB, ECAP = S::ECAP;
+  constexpr int NT = S::NT, NW = S::NW, NB = S::NB;
   static_assert(TW >= 4 && 32 % TW == 0 && NT % 32 == 0, "a warp holds whole runs of TW columns");
-  static_assert(NB <= 2048 && TW <= 32, "event fields");
+  static_assert(TW <= 8, "event fields: tile column in 3 bits");
   static_assert(NB % NT == 0, "a block's depth-table entries split evenly over the threads");
 
   extern __shared__ __align__(1024) unsigned char smem[];
   float *lut = reinterpret_cast<float *>(smem);
   float4 *zt = reinterpret_cast<float4 *>(smem + S::lut_bytes);
   float *zv = reinterpret_cast<float *>(smem + S::lut_bytes + S::zl_bytes);
-  uint32_t *evq = reinterpret_cast<uint32_t *>(smem + S::lut_bytes + S::zl_bytes + S::zi_bytes);
-  int *wtot =
-      reinterpret_cast<int *>(smem + S::lut_bytes + S::zl_bytes + S::zi_bytes + S::ev_bytes);
+  int *wtot = reinterpret_cast<int *>(smem + S::lut_bytes + S::zl_bytes + S::zi_bytes);
   int *mcol = wtot + NW * TW;
-  /* [0], [1] events of the even / odd block, [2] next item, [3] every column
-   * at row 0 after the block */
+  /* [0] events of the tile, [2] next item, [3] every column at row 0 after
+   * the block */
   int *scal = mcol + 2 * TW;
   uint32_t *stage = reinterpret_cast<uint32_t *>(smem + S::fixed_bytes);
+  /* the tile's event list, after the stage sized for the launch's tallest view */
+  uint32_t *evq = stage + S::stage_bytes(P.stride_max) / 4;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int c = tid % TW; /* the thread's column within the tile (lane % TW) */
@@ -982,16 +986,16 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
         zv[half * NB + p] = iz;
       }
     };
-    /* colour the events of the block in buffer half, each at its row */
-    /* (kbc: the first depth of that block, for the optional epilogue) */
-    auto colour_list = [&](auto c2tag, int half, int kbc) {
+    /* colour the tile's listed events, each at its row (the depth-table
+     * entries from global memory: the list spans every block) */
+    auto colour_list = [&](auto c2tag) {
       constexpr bool C2 = decltype(c2tag)::value;
-      const int ne = scal[half];
+      const int ne = scal[0];
       if (P.stats && tid == 0) n_events += (uint32_t)ne;
       for (int e = tid; e < ne; e += NT) {
-        const uint32_t ev = evq[half * ECAP + e];
-        const int kl = (int)(ev >> 21), ec = (int)((ev >> 16) & 31u), er = (int)(ev & 0xFFFFu);
-        const float4 L = zt[half * NB + (kl % U) * TPC + kl / U];
+        const uint32_t ev = evq[e];
+        const int k = (int)(ev >> 15), ec = (int)((ev >> 12) & 7u), er = (int)(ev & 0xFFFu);
+        const float4 L = __ldg(zl + k);
         const float2 xy =
             axpy2((float)(c0 + ec), make_float2(L.z, L.w), make_float2(L.x, L.y));
         uint32_t colour = CF ? color_bilinear<C2>(M, chan, xy.x, xy.y)
@@ -999,7 +1003,7 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
         if constexpr (FX) {
           if (Vp->flags & (FSV_SHADE | FSV_FOG)) {
             /* depth of sample k, as the depth table computes it */
-            const float fi = (float)(kbc + kl + 1);
+            const float fi = (float)(k + 1);
             const float z = fm(fd(fi, 2.0f), fa(fm(2.0f, Vp->z0), fm(fs(fi, 1.0f), Vp->d)));
             colour = apply_effects(chan, *Vp, colour, z);
           }
@@ -1008,16 +1012,10 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
       }
     };
     const bool cp2 = M.cpow2 != 0;
-    auto colour_events = [&](int half, int kbc) {
-      if (cp2)
-        colour_list(BoolTag<true>{}, half, kbc);
-      else
-        colour_list(BoolTag<false>{}, half, kbc);
-    };
 
     /* a column past the frame's right edge starts (and stays) at row 0 */
     if (tid < TW) mcol[tid] = (c0 + tid < W) ? H : 0;
-    if (tid == 0) scal[0] = scal[1] = 0;
+    if (tid == 0) scal[0] = 0;
     if (!(param_view && iter == 0)) {
       for (int e = tid; e < H * TW; e += NT) stage[e] = gap;
       load_table(0, 0);
@@ -1091,7 +1089,6 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
           rows(BoolTag<false>{});
         if (P.stats) n_samples += (uint32_t)max(0, min(U, n - kb - j * U));
       }
-      if (kb > 0) colour_events(par ^ 1, kb - NB);
       int run = H;
 #pragma unroll
       for (int i = 0; i < U; i++) run = min(run, r[i]);
@@ -1162,14 +1159,13 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
         const int total = __shfl_sync(FS_FULL_MASK, csum, 31);
         if (total) {
           int base = 0;
-          if (lane == 31) base = atomicAdd(&scal[par], total);
+          if (lane == 31) base = atomicAdd(&scal[0], total);
           base = __shfl_sync(FS_FULL_MASK, base, 31) + csum - cnt;
           if (cnt) {
-            uint32_t *q = evq + par * ECAP;
 #pragma unroll
             for (int i = 0; i < U; i++)
               if (r[i] < prev) {
-                q[base++] = pack_coop_event(j * U + i, c, r[i]);
+                evq[base++] = pack_coop_event(kb + j * U + i, c, r[i]);
                 prev = r[i];
               }
           }
@@ -1182,18 +1178,19 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
           zv[(par ^ 1) * NB + tid + q * NT] = iznext[q];
         }
       }
-      if (tid == 0) scal[par ^ 1] = 0; /* the previous block's list is coloured */
       __syncthreads();
 
       /* the last block, every column at row 0, or no event possible in any
-       * later block: colour this block and finish */
+       * later block */
       bool done = !more;
       if (more) done = scal[3] != 0 || tile_rest;
-      if (done) {
-        colour_events(par, kb);
-        break;
-      }
+      if (done) break;
     }
+    /* every block's events are listed: colour them into the stage */
+    if (cp2)
+      colour_list(BoolTag<true>{});
+    else
+      colour_list(BoolTag<false>{});
     __syncthreads();
 
     /* fill_vline + sky (fut/voxel_renderer.fut:246-248) over the tile: thread

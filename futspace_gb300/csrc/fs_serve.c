@@ -260,7 +260,7 @@ int fs_server_new(fs_ctx *ctx, fs_server **out, const fs_map *const *maps, int32
     fs_server_free(s);
     return fs_fail(ctx, FS_ERR_ARG, "serving needs a compiled direct-paint configuration");
   }
-  s->use_coop = c.tw && fsk_tune_supported(&c);
+  s->use_coop = c.tw && fsk_tune_supported(&c) && fs_coop_depths_ok(&c, cfg->max_depths);
   if (cfg->tune[0] && cfg->tune[3] == 2 && !s->use_coop) {
     fs_server_free(s);
     return fs_fail(ctx, FS_ERR_ARG, "no cooperative tile compiled for this mode");

@@ -198,7 +198,8 @@ int fs_plan_autotune(fs_plan *p, int32_t reps, int32_t out5[5], float *best_ms) 
     fs_tune_get(i, t5);
     FsTune t = {t5[0], t5[1], t5[2], t5[3], 0, (p->fv_h[0].flags & FSV_SMOOTH) ? 1 : 0,
                 (p->fv_h[0].flags & (FSV_SHADE | FSV_FOG)) ? 1 : 0};
-    if (!fs_tune_fits(ctx, &t, p->stride_max)) continue;
+    if (!fs_tune_fits(ctx, &t, p->stride_max) || !fs_coop_depths_ok(&t, fs_plan_max_depths(p)))
+      continue;
     rc = fs_plan_set_tune(p, t5);
     if (rc) break;
     float ms = 0.0f;
