@@ -260,28 +260,29 @@ def measured_peaks() -> dict:
 
 
 def capture_figures(name: str, tune) -> dict:
-    """Per-launch ncu figures (`key: value` lines) from the committed summary of
-    workload `name`, only when it was captured with the kernel configuration
-    this run uses (its `capture_tune:` line); else {} -- a summary of another
-    configuration says nothing about this launch."""
+    """Per-launch ncu figures from the committed summary of workload `name`:
+    its `capture TW,LC,U,STAGE: key value ...` line for the kernel
+    configuration this run uses, else {} -- a capture of another configuration
+    says nothing about this launch."""
     p = ROOT / "profiles" / f"render_{name}.md"
     if not p.exists():
         return {}
-    vals = {}
-    for line in p.read_text().splitlines():
-        if ":" in line and not line.startswith((" ", "|", "#")):
-            k, v = line.split(":", 1)
-            vals[k.strip()] = v.strip()
     want = ",".join(str(int(x)) for x in tune[:4])
-    if vals.get("capture_tune", "").replace(" ", "") != want:
-        return {}
-    out = {"capture_tune": want}
-    for k in ("dram_bytes_per_launch", "l2_read_sectors_per_launch"):
-        try:
-            out[k] = float(vals[k].split()[0])
-        except (KeyError, ValueError, IndexError):
-            pass
-    return out
+    for line in p.read_text().splitlines():
+        if not line.startswith("capture ") or ":" not in line:
+            continue
+        head, body = line[len("capture "):].split(":", 1)
+        if head.replace(" ", "") != want:
+            continue
+        out = {"capture_tune": want}
+        words = body.split()
+        for k, v in zip(words[0::2], words[1::2]):
+            try:
+                out[k] = float(v)
+            except ValueError:
+                pass
+        return out
+    return {}
 
 
 def roofline(frame_bytes: int, s_full: int, s_eff: int, kernel_ms: float, hbm_gbs: float,
