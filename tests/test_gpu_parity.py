@@ -471,3 +471,33 @@ def test_l2_read_probe(gpu_ctx):
     """The roofline's L2 read bandwidth probe returns a finite positive rate."""
     gbs = gpu_ctx.measure_l2_read_gbs(16 << 20, 8)
     assert 100.0 < gbs < 1.0e6
+
+
+def test_cooperative_tile_limits(fs, orc, gpu_ctx, maps256):
+    """The cooperative tile's event list holds a whole tile's events (at most
+    TW x H): a 3000-row frame through the 4-column tile; and views beyond its
+    32-bit event entries (more than 2^17 depths) fall back to another kernel
+    form, alone and in a plan, with the same pixels."""
+    hm, cm = maps256
+    fmap = fs.Map(gpu_ctx, hm, cm)
+    p = fs.default_params()
+    tall = fs.Camera(100.0, 100.0, 180.0, 0.7, 2900.0, 900.0, 1.2, 0xFF9090E0)
+    gpu_ctx.force_tune((4, 64, 4, 2))
+    try:
+        got = gpu_ctx.render(fmap, tall, 40, 3000)
+        assert count_diff(got, _oracle(orc, tall, p, hm, cm, 40, 3000)) == 0
+        # 131,073+ depths: D = 8.6 million map units at the default depth step
+        D = 131075.0 ** 2 / 2000.0
+        assert fs.num_depths(D) > 1 << 17
+        far = fs.Camera(60.0, 70.0, 300.0, 0.4, 24.0, D, 1.2, 0xFF9090E0)
+        got = gpu_ctx.render(fmap, far, 48, 48)
+        assert count_diff(got, _oracle(orc, far, p, hm, cm, 48, 48)) == 0
+    finally:
+        gpu_ctx.force_tune(None)
+    plan = fs.Plan(gpu_ctx, [fmap], [(far, 48, 48)])
+    with pytest.raises(fs.FsError):
+        plan.set_tune(8, 64, 8, 2)
+    plan.run()
+    assert count_diff(plan.frames()[0], _oracle(orc, far, p, hm, cm, 48, 48)) == 0
+    plan.close()
+    fmap.close()
