@@ -548,7 +548,6 @@ static const FsTune k_tune_order[] = {
     {32, 8, 4, 0, 0},  {32, 4, 4, 0, 0},  {64, 4, 4, 0, 0},  {32, 4, 8, 0, 0},
     {64, 2, 4, 0, 0},  {64, 1, 4, 0, 0},  {128, 1, 4, 0, 0}, {64, 1, 8, 0, 0},
     {128, 1, 8, 0, 0}, {4, 64, 8, 2, 0},  {8, 32, 8, 2, 0},  {4, 64, 4, 2, 0},
-    {8, 64, 16, 2, 0},
 };
 
 int fs_tune_count(void) { return (int)(sizeof(k_tune_order) / sizeof(k_tune_order[0])); }

@@ -1251,7 +1251,6 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
  * per block), stage 2 of the tuning tuple. */
 #define FS_COOP_LIST(X) \
   X(8, 64, 8)           \
-  X(8, 64, 16)          \
   X(4, 64, 8)           \
   X(8, 32, 8)           \
   X(4, 64, 4)
