@@ -402,10 +402,10 @@ __device__ __forceinline__ void render_strip(const FsLaunch &P, const FsView *Vp
     __syncwarp();
   };
 
-  /* A chunk none of whose rows lies above its column's minimum holds no
-   * event and leaves the minimum as it is (an event needs a row below the
-   * running minimum, which never exceeds m within the chunk): its per-depth
-   * scans are skipped. Warp-uniform. */
+  /* A chunk none of whose rows is smaller than its column's running minimum
+   * m holds no event and leaves m as it is (an event needs a row smaller than
+   * the minimum before it, which is at most m): its per-depth scans are
+   * skipped. Warp-uniform. */
   auto no_event = [&](const int(&r)[U]) -> bool {
     int rmin = r[0];
 #pragma unroll
