@@ -287,7 +287,7 @@ def capture_figures(name: str, tune) -> dict:
 
 def roofline(frame_bytes: int, s_full: int, s_eff: int, kernel_ms: float, hbm_gbs: float,
              l2_gbs: float, maps_fit_l2: bool, hbm_source: str, captured: dict,
-             kernel: str) -> dict:
+             kernel: str, events: int | None = None) -> dict:
     """T_roof = max(frame bytes / HBM copy peak, 20 B x depth samples / gather
     peak); frac = T_roof / kernel time. The gather peak is the L2 read rate for
     maps that fit in L2, else the HBM copy peak (the gathers fall to DRAM)."""
@@ -323,6 +323,13 @@ def roofline(frame_bytes: int, s_full: int, s_eff: int, kernel_ms: float, hbm_gb
                       "note": "the depth samples the kernel evaluated (after exact skips "
                               "and early exit)"},
     }
+    if events is not None:
+        # the earlier form: the bytes this kernel's work reads and writes (frame,
+        # a 4-byte height quad per evaluated sample, four colour texels per
+        # event) against the HBM copy peak
+        alg = frame_bytes + 4 * s_eff + 16 * events
+        out["hbm_copy_form"] = {"bytes": alg, "achieved": alg / (kernel_ms * 1e-3) / 1e9,
+                                "frac": alg / (kernel_ms * 1e-3) / 1e9 / hbm_gbs}
     sectors = captured.get("l2_read_sectors_per_launch")
     if sectors:
         t_sec = 32 * sectors / (l2_gbs * 1e6)
@@ -641,7 +648,7 @@ def single_leg(fs, ctx, args, rank: int, world: int, local: int, steps: int, war
     rl = roofline(4 * W * H, n * W, int(samples), k_ms, peaks["hbm_gbs"], l2_gbs, True,
                   peaks["source"], capture_figures("single1080", tune),
                   "the kernels of one plain call (depth table + render, the render a "
-                  "programmatic dependent launch)")
+                  "programmatic dependent launch)", int(events))
     cpu = cpu1 = None
     if rank == 0 and with_cpu and args.cpu_seconds > 0:
         cpu, cpu1 = cpu_baselines(views, hm, cm, args.cpu_seconds, oracle_params("single1080"))
@@ -821,7 +828,7 @@ def plan_leg(fs, ctx, args, name: str, rank: int, world: int, local: int, steps:
     map_bytes = hm.size * 5  # u8 heights + u32 colours, the algorithmic map set
     rl = roofline(frame_bytes, full_s, int(samples), k_ms, peaks["hbm_gbs"], l2_gbs,
                   map_bytes <= L2_BYTES, peaks["source"], capture_figures(name, tune),
-                  "render_kernel (persistent, one launch per step)")
+                  "render_kernel (persistent, one launch per step)", int(events))
 
     cpu = cpu1 = None
     if headline and rank == 0 and args.cpu_seconds > 0:

@@ -46,3 +46,9 @@ def test_roofline_is_the_slower_term_over_kernel_time():
     # a frame-store bound (few samples)
     r = bench.roofline(frame, 1000, 1000, 1.0, 6788.3, 15000.0, True, "measured", {}, "k")
     assert r["bound"] == "hbm" and r["frac"] == pytest.approx(t_frame / 1.0)
+
+
+def test_hbm_copy_form_is_kept_as_an_extra():
+    r = bench.roofline(100, 10, 5, 1.0, 1000.0, 2000.0, True, "m", {}, "k", events=2)
+    assert r["hbm_copy_form"]["bytes"] == 100 + 4 * 5 + 16 * 2
+    assert r["hbm_copy_form"]["frac"] == pytest.approx(r["hbm_copy_form"]["achieved"] / 1000.0)
