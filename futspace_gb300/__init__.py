@@ -101,15 +101,25 @@ def library_path() -> Path:
 
 
 _LIB = None
-# Live native objects, released in dependency order (plans, maps, contexts) at
-# interpreter exit, while the CUDA runtime is still up; __del__ does nothing
-# during finalisation.
+# Live native objects, released in dependency order (servers, plans, pinned
+# buffers, maps) at interpreter exit, while the CUDA runtime is still up;
+# __del__ does nothing during finalisation. Contexts are only synchronised:
+# their streams may be wrapped by other libraries' stream objects (a torch
+# ExternalStream) whose pending uses are released after this handler, and
+# destroying the stream first aborts those releases. Process teardown frees
+# the contexts.
 _LIVE: "weakref.WeakSet" = weakref.WeakSet()
 
 
 def _release_all():
     objs = list(_LIVE)
-    for kind in (Server, Plan, PinnedBuffer, Map, Context):
+    for o in objs:
+        if isinstance(o, Context):
+            try:
+                o.sync()
+            except Exception:
+                pass
+    for kind in (Server, Plan, PinnedBuffer, Map):
         for o in objs:
             if isinstance(o, kind):
                 try:
