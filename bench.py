@@ -57,7 +57,7 @@ MAP_SEED_H, MAP_SEED_C, VIEW_SEED = 7, 8, 20240601
 METRIC = "Gpix/s (bit-exact voxel-space frames), batched multi-view"
 METRIC_SINGLE = "Gpix/s (bit-exact voxel-space frames), one 1920x1080 frame per plain call"
 L2_POLICY = "GPU arm: L2 flushed between timed steps (256 MB write)"
-L2_BYTES = 126 << 20  # GB300 L2 capacity the driver reports
+L2_BYTES = 126 << 20  # GB300 L2 capacity (cudaDevAttrL2CacheSize)
 GATHER_BYTES_PER_SAMPLE = 20  # one 4-byte height quad + four 4-byte colour texels
 
 
