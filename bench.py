@@ -57,6 +57,8 @@ MAP_SEED_H, MAP_SEED_C, VIEW_SEED = 7, 8, 20240601
 METRIC = "Gpix/s (bit-exact voxel-space frames), batched multi-view"
 METRIC_SINGLE = "Gpix/s (bit-exact voxel-space frames), one 1920x1080 frame per plain call"
 L2_POLICY = "GPU arm: L2 flushed between timed steps (256 MB write)"
+L2_POLICY_SINGLE = ("GPU arm: L2 flushed between timed steps (1 GB write, long enough that "
+                    "the call's launches are queued before the GPU reaches them)")
 L2_BYTES = 126 << 20  # GB300 L2 capacity (cudaDevAttrL2CacheSize)
 GATHER_BYTES_PER_SAMPLE = 20  # one 4-byte height quad + four 4-byte colour texels
 
@@ -135,7 +137,7 @@ def make_workload(gen, name: str, rank: int):
             "workload": "single1080: one 1920x1080 frame per step through the plain per-frame "
                         "call (fs_render_device), cameras of the 64-frame walk in turn, D=3000, "
                         "4096^2 maps",
-            "views": 1, "map": "4096x4096 u8 heights + u32 colours", "l2": L2_POLICY}
+            "views": 1, "map": "4096x4096 u8 heights + u32 colours", "l2": L2_POLICY_SINGLE}
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -576,7 +578,10 @@ def single_leg(fs, ctx, args, rank: int, world: int, local: int, steps: int, war
     samples, events = ctx.stats(False)
     samples /= len(cams)
     events /= len(cams)
-    flush = torch.empty(64 * 1024 * 1024, dtype=torch.int32, device=dev)
+    # L2 flush between frames: 1 GB, whose write outlasts the host's submission of
+    # the next call (Python and ctypes overhead included), so the events bracket
+    # device execution rather than the GPU waiting for the host's second launch
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.int32, device=dev)
     ctx.set_option("time", 1)
     for i in range(warmup):
         ctx.render_device(fmap, cams[i % len(cams)], W, H, out.data_ptr())
@@ -788,6 +793,23 @@ def plan_leg(fs, ctx, args, name: str, rank: int, world: int, local: int, steps:
                "h2d_bytes_per_step": 96 * len(views),  # one 96-byte view record per camera
                "d2h_bytes_per_step": 4 * plan.total_pixels,
                "ms_per_step": e2e_ms, "groups": args.e2e_groups}
+        # the ceiling of this form: the device-to-host copy of the same frames
+        # alone (fs_plan_download into the same pinned buffer)
+        t_copy = []
+        for i in range(4):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            plan.download(host.numpy().view(np.uint32))
+            b.record(stream)
+            b.synchronize()
+            if i:
+                t_copy.append(a.elapsed_time(b))
+        copy_ms = float(np.median(t_copy))
+        e2e["host_link"] = {"copy_ms": copy_ms,
+                            "gbs": 4 * plan.total_pixels / copy_ms / 1e6,
+                            "ceiling": px / copy_ms / 1e6,
+                            "frac": copy_ms / e2e_ms}
 
     # the kernel forms on this plan, one configuration each (the autotuner
     # times every compiled configuration; these are the best-known of each
