@@ -1192,7 +1192,6 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
       mstart = mnext;
       if (!more || all_zero || tile_rest) break;
     }
-    /* every warp's events are listed */
     __syncthreads();
     /* every block's events are listed: colour them into the stage */
     if (cp2)
