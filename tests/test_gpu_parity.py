@@ -447,6 +447,39 @@ def test_cooperative_tile_1080p_frame(fs, orc, gpu_ctx):
         assert not bad, (tune, bad)
 
 
+def test_cooperative_tile_block_boundaries(fs, orc, gpu_ctx, maps256):
+    """Depth counts at the cooperative tile's block boundaries (one block short
+    of full, exactly one or two 512-depth blocks, one depth past them, 256-depth
+    blocks likewise), plain and as one plan whose persistent CTAs take several
+    tiles of different views in turn."""
+    hm, cm = maps256
+    fmap = fs.Map(gpu_ctx, hm, cm)
+    p = fs.default_params()
+    views = []
+    for k, n in enumerate((300, 256, 257, 511, 512, 513, 1024, 1025)):
+        D = 0.001 * n * n / 2.0  # the middle of the distances that give n depths
+        assert fs.num_depths(D) == n
+        cam = fs.gen_cameras(300 + k, hm, 1, above=(10, 40), distance=(D, D), screen_h=72)[0]
+        views.append((cam, 88 if k % 2 else 96, 72))
+    refs = [_oracle(orc, c, p, hm, cm, w, h) for c, w, h in views]
+    coop = [t for t in fs.tune_table() if t[3] == 2]
+    try:
+        for tune in coop:
+            gpu_ctx.force_tune(tune)
+            for (c, w, h), ref in zip(views, refs):
+                assert count_diff(gpu_ctx.render(fmap, c, w, h), ref) == 0, (tune, c.distance)
+    finally:
+        gpu_ctx.force_tune(None)
+    plan = fs.Plan(gpu_ctx, [fmap], views)
+    for tune in coop:
+        plan.set_tune(*tune[:3], 2, 8)  # 8 persistent CTAs: several tiles each
+        plan.run()
+        bad = [i for i, (f, r) in enumerate(zip(plan.frames(), refs)) if count_diff(f, r)]
+        assert not bad, (tune, bad)
+    plan.close()
+    fmap.close()
+
+
 def test_plain_call_kernel_timer(fs, gpu_ctx, maps256):
     """Option "time": events around the render kernels of a plain call; no pixel
     changes, and reading the timer before any timed call is a state error."""
