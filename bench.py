@@ -914,7 +914,7 @@ def main():
                     help="pin the kernel configuration of the main workload: tile_width,"
                          "lanes_per_column,depth_per_lane,stage (skips the autotuner)")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--e2e-groups", type=int, default=8,
+    ap.add_argument("--e2e-groups", type=int, default=16,
                     help="view groups of the pipelined render + download in the e2e timing")
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
