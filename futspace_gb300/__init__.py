@@ -182,6 +182,7 @@ def lib():
     _sig(L, "fs_plan_total_pixels", i64, [vp])
     _sig(L, "fs_plan_download", C.c_int, [vp, vp])
     _sig(L, "fs_plan_run_download", C.c_int, [vp, vp, i32])
+    _sig(L, "fs_plan_download_bytes", C.c_int, [vp, P(i64), P(i64)])
     _sig(L, "fs_plan_get_tune", C.c_int, [vp, P(i32)])
     _sig(L, "fs_plan_set_tune", C.c_int, [vp, P(i32)])
     _sig(L, "fs_plan_signature", C.c_int, [vp, P(i64)])
@@ -352,6 +353,8 @@ class Context:
                 lib().fs_ctx_free(self._h)
                 self._h = C.c_void_p()
             raise FsError(rc, msg or "fs_ctx_new")
+        # maps, plans and servers made on this context: closed before it
+        self._deps: "weakref.WeakSet" = weakref.WeakSet()
         _LIVE.add(self)
 
     @property
@@ -411,7 +414,13 @@ class Context:
         return int(out[0]), int(out[1])
 
     def close(self):
+        """Frees the context after the servers, plans and maps made on it."""
         if self._h:
+            deps = list(self._deps)
+            for kind in (Server, Plan, Map):
+                for o in deps:
+                    if isinstance(o, kind):
+                        o.close()
             lib().fs_ctx_free(self._h)
             self._h = C.c_void_p()
 
@@ -477,6 +486,7 @@ class Map:
         ctx.check(fn(ctx.handle, C.byref(self._h), _ptr(h), _ptr(c), h.shape[0], h.shape[1]),
                   "fs_map_new")
         self.shape = h.shape
+        ctx._deps.add(self)
         _LIVE.add(self)
 
     @classmethod
@@ -490,6 +500,7 @@ class Map:
         r, c = C.c_int64(), C.c_int64()
         lib().fs_map_shape(m._h, C.byref(r), C.byref(c))
         m.shape = (r.value, c.value)
+        ctx._deps.add(m)
         _LIVE.add(m)
         return m
 
@@ -533,6 +544,7 @@ class Plan:
                                     C.byref(self.params), arr, len(views)), "fs_plan_new")
         self.sizes = [(v[1], v[2]) for v in views]
         self.nviews = len(views)
+        ctx._deps.add(self)
         _LIVE.add(self)
 
     @property
@@ -579,6 +591,14 @@ class Plan:
         self.ctx.check(lib().fs_plan_run_download(self._h, _ptr(out), groups),
                        "fs_plan_run_download")
         return out
+
+    def download_bytes(self) -> tuple[int, int]:
+        """(bytes copied device to host, bytes of sky rows written on the host) of
+        the last run_download."""
+        copied, filled = C.c_int64(), C.c_int64()
+        self.ctx.check(lib().fs_plan_download_bytes(self._h, C.byref(copied), C.byref(filled)),
+                       "fs_plan_download_bytes")
+        return copied.value, filled.value
 
     def frames(self, flat: np.ndarray | None = None) -> list[np.ndarray]:
         flat = self.download() if flat is None else flat
@@ -669,6 +689,7 @@ class Server:
         mp = (C.c_void_p * len(maps))(*[m.handle.value for m in maps])
         ctx.check(lib().fs_server_new(ctx.handle, C.byref(self._h), mp, len(maps),
                                       C.byref(self.params), C.byref(cfg)), "fs_server_new")
+        ctx._deps.add(self)
         _LIVE.add(self)
 
     def run(self, requests, realtime: bool = False) -> dict:

@@ -79,7 +79,8 @@ def build_library(verbose: bool = False) -> Path:
         objs.append(obj)
         if not _newer(obj, [src] + hdrs):
             jobs.append(["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-fPIC", "-ffp-contract=off",
-                         "-Wall", "-Wno-unused-function", *inc, "-c", str(src), "-o", str(obj)])
+                         "-fopenmp", "-Wall", "-Wno-unused-function", *inc, "-c", str(src),
+                         "-o", str(obj)])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(8, os.cpu_count() or 1))) as ex:
         for f in [ex.submit(_run, j) for j in jobs]:
             f.result()
@@ -88,8 +89,8 @@ def build_library(verbose: bool = False) -> Path:
         if not libdir.exists():
             libdir = ch / "lib"
         tmp = LIB.with_suffix(".so.tmp")
-        _run([nvcc, ARCH, "-shared", "-cudart", "shared", "-o", str(tmp), *map(str, objs),
-              "-L", str(libdir), f"-Xlinker=-rpath={libdir}", "-lm"])
+        _run([nvcc, ARCH, "-shared", "-cudart", "shared", "-Xcompiler", "-fopenmp", "-o",
+              str(tmp), *map(str, objs), "-L", str(libdir), f"-Xlinker=-rpath={libdir}", "-lm"])
         os.replace(tmp, LIB)
     if verbose:
         print(f"built {LIB}", file=sys.stderr)

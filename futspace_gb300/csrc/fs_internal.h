@@ -102,6 +102,10 @@ typedef struct {
   const float *zinvz;          /* per depth: inv_z */
   int32_t *head;               /* persistent work counter; NULL: one item per CTA */
   unsigned long long *stats;   /* optional counters: samples, events; NULL: off */
+  /* per view (index into `views`, 0 for view0): atomicMin of the final minimum
+   * row of each of its columns, so rows [0, value) are sky in every column;
+   * NULL: off */
+  int32_t *sky_rows;
   int32_t nitems;
   int32_t stride_max;          /* stage column stride (>= max H, odd) */
   int32_t pad[2];

@@ -40,9 +40,14 @@ void fs_plan_free(fs_plan *p) {
   plan_release_graph(p);
   for (int i = 0; i < 2; i++)
     if (p->ev_render[i]) cudaEventDestroy(p->ev_render[i]);
-  for (int i = 0; i < FS_PLAN_MAX_GROUPS; i++)
+  for (int i = 0; i < FS_PLAN_MAX_GROUPS; i++) {
     if (p->grp_done[i]) cudaEventDestroy(p->grp_done[i]);
+    if (p->grp_meta[i]) cudaEventDestroy(p->grp_meta[i]);
+  }
   if (p->copy_stream) cudaStreamDestroy(p->copy_stream);
+  if (p->meta_stream) cudaStreamDestroy(p->meta_stream);
+  cudaFree(p->sky_d);
+  cudaFreeHost(p->sky_h);
   cudaFree(p->grp_items_d);
   cudaFree(p->grp_heads_d);
   free(p->items_h);
@@ -513,11 +518,56 @@ static int plan_build_groups(fs_plan *p, int32_t groups) {
   if (!e && !p->grp_heads_d)
     e = cudaMalloc((void **)&p->grp_heads_d, sizeof(int32_t) * FS_PLAN_MAX_GROUPS);
   if (!e && !p->copy_stream) e = cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking);
-  for (int g = 0; !e && g < FS_PLAN_MAX_GROUPS; g++)
+  if (!e && !p->meta_stream) e = cudaStreamCreateWithFlags(&p->meta_stream, cudaStreamNonBlocking);
+  if (!e && !p->sky_d) e = cudaMalloc((void **)&p->sky_d, sizeof(int32_t) * (size_t)p->nviews);
+  if (!e && !p->sky_h) e = cudaMallocHost((void **)&p->sky_h, sizeof(int32_t) * (size_t)p->nviews);
+  for (int g = 0; !e && g < FS_PLAN_MAX_GROUPS; g++) {
     if (!p->grp_done[g]) e = cudaEventCreateWithFlags(&p->grp_done[g], cudaEventDisableTiming);
+    if (!e && !p->grp_meta[g])
+      e = cudaEventCreateWithFlags(&p->grp_meta[g], cudaEventDisableTiming);
+  }
   if (e) return fs_cuda_fail(ctx, e, "group set-up");
   p->ngroups = groups;
   return FS_OK;
+}
+
+/* Writes `value` to n consecutive u32 (16-byte stores after a short head). */
+static void fill_u32(uint32_t *dst, int64_t n, uint32_t value) {
+  while (n > 0 && ((uintptr_t)dst & 15u)) {
+    *dst++ = value;
+    n--;
+  }
+  const uint32_t v4[4] = {value, value, value, value};
+  for (int64_t i = 0; i < n / 4; i++) memcpy(dst + 4 * i, v4, sizeof(v4));
+  for (int64_t i = n & ~(int64_t)3; i < n; i++) dst[i] = value;
+}
+
+/* The sky rows [0, s_v) of views [v0, v1) of `host` (frames at the plan's
+ * offsets): split into pieces of at most 256 K pixels, written by the host's
+ * threads. Returns the bytes written. */
+static int64_t fill_sky_rows(const fs_plan *p, uint32_t *host, int32_t v0, int32_t v1) {
+  enum { PIECE = 256 * 1024 };
+  int64_t pieces = 0, bytes = 0;
+  for (int32_t v = v0; v < v1; v++) {
+    const int64_t px = (int64_t)p->sky_h[v] * p->fv_h[v].W;
+    pieces += (px + PIECE - 1) / PIECE;
+    bytes += 4 * px;
+  }
+#pragma omp parallel for schedule(dynamic, 1)
+  for (int64_t k = 0; k < pieces; k++) {
+    /* the piece's view: walk the group's views (a few dozen) */
+    int64_t base = 0;
+    int32_t v = v0;
+    for (;; v++) {
+      const int64_t np = ((int64_t)p->sky_h[v] * p->fv_h[v].W + PIECE - 1) / PIECE;
+      if (k < base + np) break;
+      base += np;
+    }
+    const int64_t px = (int64_t)p->sky_h[v] * p->fv_h[v].W;
+    const int64_t a = (k - base) * PIECE, b = a + PIECE < px ? a + PIECE : px;
+    fill_u32(host + p->offsets[v] + a, b - a, p->fv_h[v].sky);
+  }
+  return bytes;
 }
 
 int fs_plan_run_download(fs_plan *p, uint32_t *host, int32_t groups) {
@@ -539,16 +589,20 @@ int fs_plan_run_download(fs_plan *p, uint32_t *host, int32_t groups) {
     if (p->ncap[v] > max_n) max_n = p->ncap[v];
   int e = cudaMemsetAsync(p->grp_heads_d, 0, sizeof(int32_t) * (size_t)groups, ctx->stream);
   if (!e) e = cudaMemsetAsync(p->head_d, 0, 2 * sizeof(int32_t), ctx->stream);
+  /* every view's all-sky row count starts above any frame height */
+  if (!e) e = cudaMemsetAsync(p->sky_d, 0x7F, sizeof(int32_t) * (size_t)p->nviews, ctx->stream);
   if (!e) e = fsk_ztable(p->fv_d, NULL, p->nviews, max_n, p->zline, p->zinvz, ctx->stream);
   if (!e) e = plan_segmin(p);
   const int32_t per_cta = fsk_items_per_cta(&p->tune);
   const FsTune kt = plan_kernel_tune(p);
+  /* every group's render, then its views' sky rows to the host */
   for (int g = 0; !e && g < groups; g++) {
     FsLaunch L;
     plan_fill_launch(p, &L);
     L.items = p->grp_items_d + p->grp_item_off[g];
     L.nitems = p->grp_item_off[g + 1] - p->grp_item_off[g];
     L.head = p->grp_heads_d + g;
+    L.sky_rows = p->sky_d;
     int32_t grid = (L.nitems + per_cta - 1) / per_cta;
     if (grid > p->grid) grid = p->grid;
     if (L.nitems > 0) e = fsk_render(&L, &kt, p->hf, p->cf, grid, ctx->stream);
@@ -556,16 +610,47 @@ int fs_plan_run_download(fs_plan *p, uint32_t *host, int32_t groups) {
       e = fsk_gapfill(p->fv_d + p->grp_first[g], NULL, p->grp_first[g + 1] - p->grp_first[g],
                       p->wmax, ctx->stream);
     if (!e) e = cudaEventRecord(p->grp_done[g], ctx->stream);
-    if (!e) e = cudaStreamWaitEvent(p->copy_stream, p->grp_done[g], 0);
-    const int64_t a = p->offsets[p->grp_first[g]];
-    const int64_t b = p->grp_first[g + 1] < p->nviews ? p->offsets[p->grp_first[g + 1]] : p->total_px;
-    if (!e && b > a)
-      e = cudaMemcpyAsync(host + a, p->frames + a, sizeof(uint32_t) * (size_t)(b - a),
-                          cudaMemcpyDeviceToHost, p->copy_stream);
+    if (!e) e = cudaStreamWaitEvent(p->meta_stream, p->grp_done[g], 0);
+    const int32_t v0 = p->grp_first[g], v1 = p->grp_first[g + 1];
+    if (!e)
+      e = cudaMemcpyAsync(p->sky_h + v0, p->sky_d + v0, sizeof(int32_t) * (size_t)(v1 - v0),
+                          cudaMemcpyDeviceToHost, p->meta_stream);
+    if (!e) e = cudaEventRecord(p->grp_meta[g], p->meta_stream);
   }
   ctx->launches += 1 + groups + (p->nsegitems ? 1 : 0) + (p->segbuf_d ? groups : 0);
+  /* per group, once its sky rows are known: the rows below them cross the
+   * link (one copy per view, after the group's render), and the host's
+   * threads write the sky rows meanwhile */
+  int64_t copied = 4 * (int64_t)p->nviews, filled = 0;
+  for (int g = 0; !e && g < groups; g++) {
+    const int32_t v0 = p->grp_first[g], v1 = p->grp_first[g + 1];
+    e = cudaEventSynchronize(p->grp_meta[g]);
+    if (!e) e = cudaStreamWaitEvent(p->copy_stream, p->grp_done[g], 0);
+    for (int32_t v = v0; !e && v < v1; v++) {
+      const int32_t H = p->fv_h[v].H, W = p->fv_h[v].W;
+      int32_t s = p->sky_h[v];
+      s = s < 0 ? 0 : (s > H ? H : s);
+      p->sky_h[v] = s;
+      const int64_t a = p->offsets[v] + (int64_t)s * W, px = (int64_t)(H - s) * W;
+      if (px > 0) {
+        e = cudaMemcpyAsync(host + a, p->frames + a, sizeof(uint32_t) * (size_t)px,
+                            cudaMemcpyDeviceToHost, p->copy_stream);
+        copied += 4 * px;
+      }
+    }
+    if (!e) filled += fill_sky_rows(p, host, v0, v1);
+  }
   if (!e) e = cudaStreamSynchronize(p->copy_stream);
   if (e) return fs_cuda_fail(ctx, e, "pipelined render and download");
+  p->dl_copied = copied;
+  p->dl_filled = filled;
+  return FS_OK;
+}
+
+int fs_plan_download_bytes(const fs_plan *p, int64_t *copied, int64_t *filled) {
+  if (!p) return FS_ERR_ARG;
+  if (copied) *copied = p->dl_copied;
+  if (filled) *filled = p->dl_filled;
   return FS_OK;
 }
 

@@ -107,6 +107,14 @@ struct fs_plan {
   int32_t *grp_heads_d;
   cudaStream_t copy_stream;
   cudaEvent_t grp_done[FS_PLAN_MAX_GROUPS];
+  /* per view, the rows at the top that are sky in every column (the render
+   * kernels' atomicMin of the columns' final minimum rows): only the rows
+   * below them cross the device-to-host link, the host writes the sky rows */
+  int32_t *sky_d;
+  int32_t *sky_h;                           /* pinned */
+  cudaStream_t meta_stream;                 /* the group's sky rows to the host */
+  cudaEvent_t grp_meta[FS_PLAN_MAX_GROUPS];
+  int64_t dl_copied, dl_filled;             /* bytes of the last run_download */
 };
 
 int fs_fail(fs_ctx *ctx, int code, const char *fmt, ...);

@@ -43,6 +43,8 @@
  * with too few columns to keep the GPU busy.
  */
 #pragma once
+#include <climits>
+
 #include "fs_device.cuh"
 
 namespace fsd {
@@ -603,6 +605,17 @@ __device__ __forceinline__ const FsView *decode_item(const FsLaunch &P, int item
   return &P.view0;
 }
 
+/* A warp's columns' final minimum rows (m, INT_MAX for a lane whose column is
+ * past the frame) into the view's all-sky row count: rows above a column's
+ * final minimum are sky, so rows [0, min over columns) are sky in every
+ * column of the frame. Off unless the launch asks for it. */
+__device__ __forceinline__ void note_sky_rows(const FsLaunch &P, const FsView *Vp, int m,
+                                              int lane) {
+  if (!P.sky_rows) return;
+  const int mv = (int)__reduce_min_sync(FS_FULL_MASK, (unsigned)m);
+  if (lane == 0) atomicMin(P.sky_rows + (P.views ? (int)(Vp - P.views) : 0), mv);
+}
+
 template <int TW, int LC, int U, int HF, int CF, int STG, int SM, int FX, int SEG>
 __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_blocks))
     render_kernel(const __grid_constant__ FsLaunch P) {
@@ -657,6 +670,7 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
       render_strip<TW, LC, U, HF, CF, STG, SM, FX>(P, Vp, c0, cl, lane, lanemask_lt, q, stage,
                                                    chan, 0, Vp->n, H, m, gapcols, n_samples,
                                                    n_events);
+      note_sky_rows(P, Vp, c0 + cl < W ? m : INT_MAX, lane);
       /* gap fill + sky for this warp's columns, then the transposed store */
 #pragma unroll 1
       for (int c = 0; c < CPW; c++) {
@@ -701,6 +715,8 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
       render_strip<TW, LC, U, HF, CF, STG, SM, FX>(P, Vp, c0, cl, lane, lanemask_lt, q, stage,
                                                    chan, kb, ke, m0, m, gapcols, n_samples,
                                                    n_events);
+      /* an earlier segment's minimum is no smaller than the column's final one */
+      note_sky_rows(P, Vp, col < W ? m : INT_MAX, lane);
       const uint32_t sky = Vp->sky, gap = Vp->gap;
       uint32_t *const out = Vp->out;
       if (SEG && nseg > 1) {
@@ -1192,6 +1208,9 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
       mstart = mnext;
       if (!more || all_zero || tile_rest) break;
     }
+    /* the columns' final minima (no later block lowers them); a warp holds
+     * every column of the tile */
+    if (warp == 0) note_sky_rows(P, Vp, c0 + c < W ? mstart : INT_MAX, lane);
     __syncthreads();
     /* every block's events are listed: colour them into the stage */
     if (cp2)

@@ -214,12 +214,18 @@ int64_t fs_plan_total_pixels(const fs_plan *plan);
 /* Copies every frame to `host` (fs_plan_total_pixels u32 values, frames laid
  * out at fs_plan_frame_offset) and waits. */
 int fs_plan_download(fs_plan *plan, uint32_t *host);
-/* Renders every view and copies every frame to `host` (the fs_plan_download
+/* Renders every view and writes every frame to `host` (the fs_plan_download
  * layout), with the views split into `groups` contiguous groups of about equal
  * pixel count (1..16): group g+1 renders while group g's frames are copied, so
- * with pinned host memory the copy time mostly hides the render time. Waits
- * for the copies. */
+ * with pinned host memory the copy time mostly hides the render time. The
+ * render kernels also find, per view, the rows at the top that are sky in every
+ * column (above every column's highest terrain row); only the rows below them
+ * are copied, and the calling thread's OpenMP team writes the sky rows into
+ * `host` meanwhile (the same pixels as a full copy). Waits for the copies. */
 int fs_plan_run_download(fs_plan *plan, uint32_t *host, int32_t groups);
+/* Bytes of the last fs_plan_run_download: copied device to host (frame rows
+ * and the per-view sky row counts) and written on the host (sky rows). */
+int fs_plan_download_bytes(const fs_plan *plan, int64_t *copied, int64_t *filled);
 /* Kernel configuration the plan uses (see fs_ctx_force_tune); out5[4] is the
  * persistent grid size actually launched. */
 int fs_plan_get_tune(const fs_plan *plan, int32_t out5[5]);

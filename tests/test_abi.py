@@ -107,3 +107,32 @@ def test_tune_table(fs):
     t = fs.tune_table()
     assert len(t) >= 8 and all(len(x) == 4 for x in t)
     assert any(x[3] == 1 for x in t) and any(x[3] == 0 for x in t)
+
+
+
+def test_context_close_closes_its_objects(fs, monkeypatch):
+    """Closing a context first closes the servers, plans and maps made on it
+    (their handles refer to the context), then frees the context."""
+    import weakref
+
+    order = []
+    monkeypatch.setattr(fs.Server, "close", lambda self: order.append("server"))
+    monkeypatch.setattr(fs.Plan, "close", lambda self: order.append("plan"))
+    monkeypatch.setattr(fs.Map, "close", lambda self: order.append("map"))
+
+    class FakeLib:
+        def fs_ctx_free(self, h):
+            order.append("context")
+
+    monkeypatch.setattr(fs, "lib", lambda: FakeLib())
+    ctx = fs.Context.__new__(fs.Context)
+    ctx._h = C.c_void_p(1)
+    ctx._deps = weakref.WeakSet()
+    objs = [fs.Map.__new__(fs.Map), fs.Plan.__new__(fs.Plan), fs.Server.__new__(fs.Server)]
+    for o in objs:
+        ctx._deps.add(o)
+    ctx.close()
+    assert order == ["server", "plan", "map", "context"]
+    assert not ctx._h
+    ctx.close()  # a second close does nothing
+    assert order == ["server", "plan", "map", "context"]

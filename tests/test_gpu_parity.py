@@ -109,6 +109,52 @@ def test_batch_plan_all_configurations(fs, orc, gpu_ctx, maps1024):
         plan.set_tune(*fs.tune_table()[groups % len(fs.tune_table())])
 
 
+def test_run_download_sky_rows(fs, orc, gpu_ctx, maps256):
+    """fs_plan_run_download copies only the rows below each view's all-sky rows
+    and writes the sky rows on the host: frames identical to the oracle with
+    views whose every row is sky, views with no sky row (camera below the
+    terrain), ordinary views, a view split into depth segments, both gap
+    rules, every kernel form, pinned and pageable host buffers (stale bytes
+    overwritten), and byte counters that add up to the frames."""
+    hm, cm = maps256
+    fmap = fs.Map(gpu_ctx, hm, cm)
+    base = fs.gen_cameras(401, hm, 3, above=(20, 80), distance=(300, 900), screen_h=96)
+    views = [(base[0], 128, 96),
+             (fs.Camera(60.0, 70.0, -10.0, 0.4, 48.0, 400.0, 1.2, 0xFF9090E0), 96, 64),
+             (fs.Camera(80.0, 90.0, 120.0, 1.0, 1.0e5, 400.0, 1.2, 0xFF8080D0), 64, 48),
+             (base[1], 257, 131), (base[2], 40, 300)]
+    for gap in (0, 1):
+        p = fs.default_params(gap_rule=gap)
+        refs = [_oracle(orc, c, p, hm, cm, w, h) for c, w, h in views]
+        plan = fs.Plan(gpu_ctx, [fmap], views, params=p)
+        pinned = fs.PinnedBuffer(plan.total_pixels)
+        pageable = np.empty(plan.total_pixels, np.uint32)
+        for k, tune in enumerate(fs.tune_table()[::3] + [(8, 64, 8, 2)]):
+            plan.set_tune(*tune)
+            for groups, buf in ((1, pinned.array), (2, pageable), (5, pinned.array)):
+                buf[:] = 0x12345678
+                flat = plan.run_download(buf, groups=groups)
+                bad = [i for i, (f, r) in enumerate(zip(plan.frames(flat), refs))
+                       if count_diff(f, r)]
+                assert not bad, (gap, tune, groups, bad)
+                copied, filled = plan.download_bytes()
+                # every frame's pixels once (the arena's alignment gaps are no frame's)
+                assert copied + filled == 4 * sum(w * h for _, w, h in views) + 4 * len(views)
+                assert filled >= 4 * 64 * 48  # the all-sky view is written on the host
+        pinned.close()
+        plan.close()
+    # one small view alone: the plan splits its depths into segments
+    cam = base[0]
+    ref = _oracle(orc, cam, fs.default_params(), hm, cm, 320, 240)
+    plan = fs.Plan(gpu_ctx, [fmap], [(cam, 320, 240)])
+    for tune in ((64, 2, 4, 0), (128, 1, 4, 0), (32, 8, 4, 0)):
+        plan.set_tune(*tune)
+        out = np.full(320 * 240, 7, np.uint32)
+        assert count_diff(plan.frames(plan.run_download(out, groups=1))[0], ref) == 0, tune
+    plan.close()
+    fmap.close()
+
+
 def test_batch_two_maps_and_camera_update(fs, orc, gpu_ctx, maps1024, maps256):
     (h1, c1), (h2, c2) = maps1024, maps256
     m1, m2 = fs.Map(gpu_ctx, h1, c1), fs.Map(gpu_ctx, h2, c2)
