@@ -531,17 +531,6 @@ static int plan_build_groups(fs_plan *p, int32_t groups) {
   return FS_OK;
 }
 
-/* Writes `value` to n consecutive u32 (16-byte stores after a short head). */
-static void fill_u32(uint32_t *dst, int64_t n, uint32_t value) {
-  while (n > 0 && ((uintptr_t)dst & 15u)) {
-    *dst++ = value;
-    n--;
-  }
-  const uint32_t v4[4] = {value, value, value, value};
-  for (int64_t i = 0; i < n / 4; i++) memcpy(dst + 4 * i, v4, sizeof(v4));
-  for (int64_t i = n & ~(int64_t)3; i < n; i++) dst[i] = value;
-}
-
 /* The sky rows [0, s_v) of views [v0, v1) of `host` (frames at the plan's
  * offsets): split into pieces of at most 256 K pixels, written by the host's
  * threads. Returns the bytes written. */
@@ -565,7 +554,7 @@ static int64_t fill_sky_rows(const fs_plan *p, uint32_t *host, int32_t v0, int32
     }
     const int64_t px = (int64_t)p->sky_h[v] * p->fv_h[v].W;
     const int64_t a = (k - base) * PIECE, b = a + PIECE < px ? a + PIECE : px;
-    fill_u32(host + p->offsets[v] + a, b - a, p->fv_h[v].sky);
+    fs_fill_u32(host + p->offsets[v] + a, b - a, p->fv_h[v].sky);
   }
   return bytes;
 }

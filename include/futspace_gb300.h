@@ -171,7 +171,9 @@ int32_t fs_num_depths(float distance, const fs_params *params);
 int fs_render_device(fs_ctx *ctx, const fs_map *map, const fs_camera *cam,
                      const fs_params *params, int32_t width, int32_t height,
                      uint32_t *out_dev);
-/* Same into HOST memory `out_host`: renders, copies the frame back and waits. */
+/* Same into HOST memory `out_host`: renders, then copies the rows below the
+ * frame's leading all-sky rows back while the calling thread's OpenMP team
+ * writes the sky rows, and waits. */
 int fs_render(fs_ctx *ctx, const fs_map *map, const fs_camera *cam, const fs_params *params,
               int32_t width, int32_t height, uint32_t *out_host);
 /* Allocation-free variant of fs_render_device (no counterpart in the
