@@ -215,20 +215,6 @@ void fs_fill_u32(uint32_t *dst, int64_t n, uint32_t value) {
   for (int64_t i = n & ~(int64_t)3; i < n; i++) dst[i] = value;
 }
 
-void fs_fill_u32_team(uint32_t *dst, int64_t n, uint32_t value) {
-  enum { PIECE = 256 * 1024 };
-  const int64_t pieces = (n + PIECE - 1) / PIECE;
-  if (pieces <= 1) {
-    fs_fill_u32(dst, n, value);
-    return;
-  }
-#pragma omp parallel for schedule(dynamic, 1)
-  for (int64_t k = 0; k < pieces; k++) {
-    const int64_t a = k * PIECE, b = a + PIECE < n ? a + PIECE : n;
-    fs_fill_u32(dst + a, b - a, value);
-  }
-}
-
 void fs_ctx_free(fs_ctx *ctx) {
   if (!ctx) return;
   cudaSetDevice(ctx->device);
@@ -236,8 +222,6 @@ void fs_ctx_free(fs_ctx *ctx) {
   cudaFree(ctx->zline);
   cudaFree(ctx->zinvz);
   cudaFree(ctx->frame_dev);
-  cudaFree(ctx->sky_d);
-  cudaFreeHost(ctx->sky_h);
   cudaFree(ctx->segbuf);
   cudaFree(ctx->stats_dev);
   if (ctx->ev_kernel[0]) cudaEventDestroy(ctx->ev_kernel[0]);
@@ -717,7 +701,6 @@ int fs_render_view(fs_ctx *ctx, const FsMapDev *map, FsView *v, const FsTune *tu
   L->zinvz = zinvz;
   /* the work counters cost instructions per depth chunk: only when collected */
   L->stats = ctx->collect_stats ? ctx->stats_dev : NULL;
-  L->sky_rows = ctx->sky_target;
   L->nitems = ntiles * v->nseg;
   L->stride_max = stride;
   /* the timer brackets every kernel of the call; an event between two of them
@@ -784,33 +767,9 @@ int fs_render(fs_ctx *ctx, const fs_map *map, const fs_camera *cam, const fs_par
       return fs_fail(ctx, FS_ERR_NOMEM, "cudaMalloc(frame %zu bytes)", bytes);
     ctx->frame_cap = bytes;
   }
-  if (!ctx->sky_d) {
-    if (cudaMalloc((void **)&ctx->sky_d, sizeof(int32_t)) != cudaSuccess ||
-        cudaMallocHost((void **)&ctx->sky_h, sizeof(int32_t)) != cudaSuccess) {
-      cudaFree(ctx->sky_d);
-      ctx->sky_d = NULL;
-      return fs_fail(ctx, FS_ERR_NOMEM, "sky row counter");
-    }
-  }
-  /* the render notes the frame's leading rows that are sky in every column:
-   * only the rows below them cross the link, the host writes the sky rows */
-  int e = cudaMemsetAsync(ctx->sky_d, 0x7F, sizeof(int32_t), ctx->stream);
-  if (e) return fs_cuda_fail(ctx, e, "sky row counter reset");
-  ctx->sky_target = ctx->sky_d;
   int rc = fs_render_device(ctx, map, cam, params, width, height, ctx->frame_dev);
-  ctx->sky_target = NULL;
   if (rc) return rc;
-  e = cudaMemcpyAsync(ctx->sky_h, ctx->sky_d, sizeof(int32_t), cudaMemcpyDeviceToHost,
-                      ctx->stream);
-  if (!e) e = cudaStreamSynchronize(ctx->stream);
-  if (e) return fs_cuda_fail(ctx, e, "sky row count");
-  int32_t s = *ctx->sky_h;
-  s = s < 0 ? 0 : (s > height ? height : s);
-  const size_t top = (size_t)s * (size_t)width;
-  if (top < (size_t)width * (size_t)height)
-    e = cudaMemcpyAsync(out_host + top, ctx->frame_dev + top, bytes - 4 * top,
-                        cudaMemcpyDeviceToHost, ctx->stream);
-  if (!e) fs_fill_u32_team(out_host, (int64_t)top, cam->sky_color);
+  int e = cudaMemcpyAsync(out_host, ctx->frame_dev, bytes, cudaMemcpyDeviceToHost, ctx->stream);
   if (!e) e = cudaStreamSynchronize(ctx->stream);
   if (e) return fs_cuda_fail(ctx, e, "frame download");
   return FS_OK;

@@ -102,10 +102,6 @@ typedef struct {
   const float *zinvz;          /* per depth: inv_z */
   int32_t *head;               /* persistent work counter; NULL: one item per CTA */
   unsigned long long *stats;   /* optional counters: samples, events; NULL: off */
-  /* per view (index into `views`, 0 for view0): atomicMin of the final minimum
-   * row of each of its columns, so rows [0, value) are sky in every column;
-   * NULL: off */
-  int32_t *sky_rows;
   int32_t nitems;
   int32_t stride_max;          /* stage column stride (>= max H, odd) */
   int32_t pad[2];
@@ -144,6 +140,11 @@ int fsk_gapfill(const FsView *views_dev, const FsView *view0, int32_t nviews, in
 int32_t fsk_items_per_cta(const FsTune *t);
 int fsk_l2_read(const void *buf, int64_t bytes, int32_t reps, int32_t grid, uint32_t *sink,
                 cudaStream_t st);
+/* Per view, into out[v] (set to INT32_MAX beforehand): the smallest row index
+ * holding a pixel other than the view's sky value, so rows [0, min(out, H))
+ * of its frame are all sky. Views from views_dev (nviews of them), or view0. */
+int fsk_sky_rows(const FsView *views_dev, const FsView *view0, int32_t nviews, int32_t max_h,
+                 int32_t *out, cudaStream_t st);
 /* A work item names a view (or serving session), a depth segment and a column
  * tile (shared-memory stage) or strip (direct painting). */
 #define FS_ITEM_VIEWS 32768

@@ -5,6 +5,7 @@
  *  - the i32 -> u8 height mask of update_map,
  *  - dispatch of the render kernel over the four filter pairs.
  */
+#include <climits>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
@@ -151,6 +152,46 @@ extern "C" int fsk_l2_read(const void *buf, int64_t bytes, int32_t reps, int32_t
                            uint32_t *sink, cudaStream_t st) {
   if (bytes < 16 || reps < 1 || grid < 1) return (int)cudaErrorInvalidValue;
   l2_read_kernel<<<grid, 512, 0, st>>>(static_cast<const uint4 *>(buf), bytes / 16, reps, sink);
+  return (int)cudaGetLastError();
+}
+
+/* The first row of a frame holding a non-sky pixel, top down: block (x, v)
+ * scans rows [x*R, x*R + R) of view v (a thread per pixel, striding), skips
+ * them when a row above is already known to hold one, and folds the first such
+ * row into out[v]. */
+constexpr int kSkyRowsPerBlock = 4;
+__global__ void sky_rows_kernel(const FsView *views, FsView view0, int32_t *out) {
+  const FsView &V = views ? views[blockIdx.y] : view0;
+  int32_t *slot = out + (views ? blockIdx.y : 0);
+  const int W = V.W, H = V.H;
+  const int r0 = blockIdx.x * kSkyRowsPerBlock;
+  if (r0 >= H) return;
+  /* the row already known to hold a non-sky pixel, read once per warp so the
+   * warp's reduction below has every lane */
+  const int known = __shfl_sync(0xffffffffu, *(volatile int32_t *)slot, 0);
+  if (r0 >= known) return;
+  const int r1 = min(H, r0 + kSkyRowsPerBlock);
+  const uint32_t sky = V.sky;
+  const uint32_t *f = V.out + (size_t)r0 * W;
+  const int n = (r1 - r0) * W;
+  int first = INT_MAX;
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+    if (__ldcs(f + i) != sky) {
+      first = r0 + i / W;
+      break;
+    }
+  first = (int)__reduce_min_sync(0xffffffffu, (unsigned)first);
+  if ((threadIdx.x & 31) == 0 && first != INT_MAX) atomicMin(slot, first);
+}
+
+extern "C" int fsk_sky_rows(const FsView *views_dev, const FsView *view0, int32_t nviews,
+                            int32_t max_h, int32_t *out, cudaStream_t st) {
+  if (nviews <= 0 || max_h <= 0) return (int)cudaSuccess;
+  FsView v0;
+  if (view0) v0 = *view0;
+  else memset(&v0, 0, sizeof(v0));
+  dim3 grid((max_h + kSkyRowsPerBlock - 1) / kSkyRowsPerBlock, views_dev ? nviews : 1);
+  sky_rows_kernel<<<grid, 256, 0, st>>>(views_dev, v0, out);
   return (int)cudaGetLastError();
 }
 

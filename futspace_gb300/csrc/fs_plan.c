@@ -591,22 +591,24 @@ int fs_plan_run_download(fs_plan *p, uint32_t *host, int32_t groups) {
     L.items = p->grp_items_d + p->grp_item_off[g];
     L.nitems = p->grp_item_off[g + 1] - p->grp_item_off[g];
     L.head = p->grp_heads_d + g;
-    L.sky_rows = p->sky_d;
     int32_t grid = (L.nitems + per_cta - 1) / per_cta;
     if (grid > p->grid) grid = p->grid;
     if (L.nitems > 0) e = fsk_render(&L, &kt, p->hf, p->cf, grid, ctx->stream);
     if (!e && p->segbuf_d)
       e = fsk_gapfill(p->fv_d + p->grp_first[g], NULL, p->grp_first[g + 1] - p->grp_first[g],
                       p->wmax, ctx->stream);
+    const int32_t v0 = p->grp_first[g], v1 = p->grp_first[g + 1];
+    /* each finished frame's leading rows that hold nothing but sky */
+    if (!e)
+      e = fsk_sky_rows(p->fv_d + v0, NULL, v1 - v0, p->stride_max, p->sky_d + v0, ctx->stream);
     if (!e) e = cudaEventRecord(p->grp_done[g], ctx->stream);
     if (!e) e = cudaStreamWaitEvent(p->meta_stream, p->grp_done[g], 0);
-    const int32_t v0 = p->grp_first[g], v1 = p->grp_first[g + 1];
     if (!e)
       e = cudaMemcpyAsync(p->sky_h + v0, p->sky_d + v0, sizeof(int32_t) * (size_t)(v1 - v0),
                           cudaMemcpyDeviceToHost, p->meta_stream);
     if (!e) e = cudaEventRecord(p->grp_meta[g], p->meta_stream);
   }
-  ctx->launches += 1 + groups + (p->nsegitems ? 1 : 0) + (p->segbuf_d ? groups : 0);
+  ctx->launches += 1 + 2 * groups + (p->nsegitems ? 1 : 0) + (p->segbuf_d ? groups : 0);
   /* per group, once its sky rows are known: the rows below them cross the
    * link (one copy per view, after the group's render), and the host's
    * threads write the sky rows meanwhile */

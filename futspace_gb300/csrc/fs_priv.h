@@ -37,9 +37,6 @@ struct fs_ctx {
   int64_t segcap;
   uint32_t *frame_dev; /* device frame for fs_render with host output */
   size_t frame_cap;
-  /* the all-sky row count of fs_render's frame (device, pinned host copy);
-   * sky_target: where the next plain render notes it (NULL: nowhere) */
-  int32_t *sky_d, *sky_h, *sky_target;
   unsigned long long *stats_dev;
   int32_t collect_stats;
   int64_t launches;
@@ -121,10 +118,8 @@ struct fs_plan {
 };
 
 int fs_fail(fs_ctx *ctx, int code, const char *fmt, ...);
-/* Writes `value` to n consecutive u32: serially, or over the calling thread's
- * OpenMP team in pieces of 256 K values. */
+/* Writes `value` to n consecutive u32 (16-byte stores after a short head). */
 void fs_fill_u32(uint32_t *dst, int64_t n, uint32_t value);
-void fs_fill_u32_team(uint32_t *dst, int64_t n, uint32_t value);
 /* Looks up the allocation-free render's scratch address on ctx's (current)
  * device into ctx->noalloc_scratch (fs_noalloc.cu). */
 int fs_noalloc_setup(fs_ctx *ctx);

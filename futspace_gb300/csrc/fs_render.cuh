@@ -43,8 +43,6 @@
  * with too few columns to keep the GPU busy.
  */
 #pragma once
-#include <climits>
-
 #include "fs_device.cuh"
 
 namespace fsd {
@@ -605,17 +603,6 @@ __device__ __forceinline__ const FsView *decode_item(const FsLaunch &P, int item
   return &P.view0;
 }
 
-/* A warp's columns' final minimum rows (m, INT_MAX for a lane whose column is
- * past the frame) into the view's all-sky row count: rows above a column's
- * final minimum are sky, so rows [0, min over columns) are sky in every
- * column of the frame. Off unless the launch asks for it. */
-__device__ __forceinline__ void note_sky_rows(const FsLaunch &P, const FsView *Vp, int m,
-                                              int lane) {
-  if (!P.sky_rows) return;
-  const int mv = (int)__reduce_min_sync(FS_FULL_MASK, (unsigned)m);
-  if (lane == 0) atomicMin(P.sky_rows + (P.views ? (int)(Vp - P.views) : 0), mv);
-}
-
 template <int TW, int LC, int U, int HF, int CF, int STG, int SM, int FX, int SEG>
 __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_blocks))
     render_kernel(const __grid_constant__ FsLaunch P) {
@@ -670,7 +657,6 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
       render_strip<TW, LC, U, HF, CF, STG, SM, FX>(P, Vp, c0, cl, lane, lanemask_lt, q, stage,
                                                    chan, 0, Vp->n, H, m, gapcols, n_samples,
                                                    n_events);
-      note_sky_rows(P, Vp, c0 + cl < W ? m : INT_MAX, lane);
       /* gap fill + sky for this warp's columns, then the transposed store */
 #pragma unroll 1
       for (int c = 0; c < CPW; c++) {
@@ -715,8 +701,6 @@ __global__ void __launch_bounds__(TW *LC, (RenderShape<TW, LC, U, STG, SM>::min_
       render_strip<TW, LC, U, HF, CF, STG, SM, FX>(P, Vp, c0, cl, lane, lanemask_lt, q, stage,
                                                    chan, kb, ke, m0, m, gapcols, n_samples,
                                                    n_events);
-      /* an earlier segment's minimum is no smaller than the column's final one */
-      note_sky_rows(P, Vp, col < W ? m : INT_MAX, lane);
       const uint32_t sky = Vp->sky, gap = Vp->gap;
       uint32_t *const out = Vp->out;
       if (SEG && nseg > 1) {
@@ -839,18 +823,14 @@ __global__ void __launch_bounds__(TW *LC, 1024 / (TW * LC)) segmin_kernel(
  *     column's threads: the thread's own U rows, a warp scan (__shfl_up_sync
  *     in steps of TW lanes) and the warp totals in shared memory; events (row
  *     below that minimum) go to the tile's event list in shared memory.
- * A block costs one CTA barrier, between A and B: the depth-table entries
- * of block b+1 are loaded into registers when block b starts and stored to
- * shared memory before its barrier (two buffers), and every thread takes its
- * column's minimum after the block from all warp totals (two buffers of
- * totals), so block b+1 starts as soon as a warp has finished block b. (A
- * third table buffer, filled by cp.async two blocks ahead, made the
- * 1920x1080 frame 23 % slower: shared memory and L1 share each SM's 256 KB,
- * and the tile's gathers need the L1; 20 KB more shared memory per CTA alone
- * cost 17 %.) A plain call (the view is a kernel parameter) computes block
- * 0's entries in the CTA and marches it while the depth-table kernel
- * finishes. The column chain is one block per step instead of one chunk, so
- * a single frame with few columns keeps every SM busy.
+ * Block b+1's depth-table entries load into registers at the end of A and go
+ * to shared memory during B (two buffers), so a block costs two barriers. A
+ * plain call (the view is a kernel parameter) computes block 0's entries in
+ * the CTA and marches it while the depth-table kernel finishes. (Copying the
+ * next block's entries with cp.async while block b marches, into a third
+ * buffer, made the 1920x1080 frame 20 % slower.) The column chain is one
+ * block per step instead of one chunk, so a single frame with few columns
+ * keeps every SM busy.
  * Colouring does not feed the march (the running minima come from rows
  * alone), so it stays off the chain of blocks: after the last block (or once
  * every column's minimum is row 0, or no later block can hold an event) every
@@ -871,8 +851,8 @@ struct CoopShape {
   static constexpr size_t lut_bytes = 256 * 4;
   static constexpr size_t zl_bytes = 2ull * NB * 16; /* two blocks' entries */
   static constexpr size_t zi_bytes = 2ull * NB * 4;
-  /* warp totals [2][NW][TW], event count, item */
-  static constexpr size_t misc_bytes = (2 * (size_t)NW * TW + 4) * 4;
+  /* warp totals [NW][TW], block-start minima [2][TW], event count, item */
+  static constexpr size_t misc_bytes = ((size_t)NW * TW + 2 * TW + 4) * 4;
   /* the stage starts on a 128-byte boundary, as do its boxes (TMA sources) */
   static constexpr size_t fixed_bytes =
       (lut_bytes + zl_bytes + zi_bytes + misc_bytes + 127) / 128 * 128;
@@ -936,8 +916,10 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
   float4 *zt = reinterpret_cast<float4 *>(smem + S::lut_bytes);
   float *zv = reinterpret_cast<float *>(smem + S::lut_bytes + S::zl_bytes);
   int *wtot = reinterpret_cast<int *>(smem + S::lut_bytes + S::zl_bytes + S::zi_bytes);
-  /* [0] events of the tile, [2] next item */
-  int *scal = wtot + 2 * NW * TW;
+  int *mcol = wtot + NW * TW;
+  /* [0] events of the tile, [2] next item, [3] every column at row 0 after
+   * the block */
+  int *scal = mcol + 2 * TW;
   uint32_t *stage = reinterpret_cast<uint32_t *>(smem + S::fixed_bytes);
   /* the tile's event list, after the stage sized for the launch's tallest view */
   uint32_t *evq = stage + S::stage_bytes(P.stride_max) / 4;
@@ -990,30 +972,21 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
     const float4 *zl = P.zline + Vp->zoff;
     const float *zi = P.zinvz + Vp->zoff;
 
-    /* the depth-table entries of block kb this thread stores: position p
-     * holds depth kb + (p % TPC) * U + p / TPC, so step i of run j reads
-     * i*TPC + j (zeros past the last depth) */
-    auto load_table = [&](int kb, float4 (&L)[NB / NT], float (&iz)[NB / NT]) {
-#pragma unroll
-      for (int q = 0; q < NB / NT; q++) {
-        const int p = tid + q * NT, e = (p % TPC) * U + p / TPC;
-        L[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        iz[q] = 0.0f;
+    /* depth-table entries of block kb into buffer half: position p holds
+     * depth kb + (p % TPC) * U + p / TPC, so step i of run j reads i*TPC + j */
+    auto load_table = [&](int kb, int half) {
+      for (int p = tid; p < NB; p += NT) {
+        const int e = (p % TPC) * U + p / TPC;
+        float4 L = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        float iz = 0.0f;
         if (kb + e < n) {
-          L[q] = __ldg(zl + kb + e);
-          iz[q] = __ldg(zi + kb + e);
+          L = __ldg(zl + kb + e);
+          iz = __ldg(zi + kb + e);
         }
+        zt[half * NB + p] = L;
+        zv[half * NB + p] = iz;
       }
     };
-    auto store_table = [&](int buf, const float4 (&L)[NB / NT], const float (&iz)[NB / NT]) {
-#pragma unroll
-      for (int q = 0; q < NB / NT; q++) {
-        zt[buf * NB + tid + q * NT] = L[q];
-        zv[buf * NB + tid + q * NT] = iz[q];
-      }
-    };
-    float4 Lnext[NB / NT];
-    float iznext[NB / NT];
     /* colour the tile's listed events, each at its row (the depth-table
      * entries from global memory: the list spans every block) */
     auto colour_list = [&](auto c2tag) {
@@ -1041,14 +1014,12 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
     };
     const bool cp2 = M.cpow2 != 0;
 
-    /* the column's minimum row at the block start; a column past the
-     * frame's right edge starts (and stays) at row 0 */
-    int mstart = (c0 + c < W) ? H : 0;
+    /* a column past the frame's right edge starts (and stays) at row 0 */
+    if (tid < TW) mcol[tid] = (c0 + tid < W) ? H : 0;
     if (tid == 0) scal[0] = 0;
     if (!(param_view && iter == 0)) {
       for (int e = tid; e < H * TW; e += NT) stage[e] = gap;
-      load_table(0, Lnext, iznext);
-      store_table(0, Lnext, iznext);
+      load_table(0, 0);
     }
     __syncthreads();
 
@@ -1057,18 +1028,14 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
      * memory), so one pass of the bound arithmetic and one round of
      * max-pyramid loads serve 32 blocks */
     int bbound = 0, bbase = -(1 << 30);
-    for (int kb = 0, buf = 0, bi = 0;; kb += NB, buf ^= 1, bi++) {
-      /* X: rows of block kb (A); the next block's entries load meanwhile (a
-       * plain call's first block marches before the depth-table kernel has
-       * finished, so its loads wait until after the rows) */
-      const bool early = !(param_view && bi == 0);
-      if (early) load_table(kb + NB, Lnext, iznext);
+    for (int kb = 0, par = 0, bi = 0;; kb += NB, par ^= 1, bi++) {
+      /* X: rows of block kb (A) with the colours of the previous block (C) */
+      const int mstart = mcol[par * TW + c];
       int r[U];
 #pragma unroll
       for (int i = 0; i < U; i++) r[i] = H;
-      const float4 *ztb = zt + buf * NB;
-      const float *zvb = zv + buf * NB;
-      int *const wt = wtot + (bi & 1) * NW * TW;
+      const float4 *ztb = zt + par * NB;
+      const float *zvb = zv + par * NB;
       /* the warp's depths [ka, kz] over its TW columns */
       const int jw = warp * (32 / TW);
       const int ka = kb + jw * U, kz = min(kb + (jw + 32 / TW) * U, n) - 1;
@@ -1133,43 +1100,47 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
         if (lane >= off) incl = min(incl, t);
       }
       const int ex = __shfl_up_sync(FS_FULL_MASK, incl, TW);
-      if (lane >= 32 - TW) wt[warp * TW + c] = incl;
-      if (!early) {
-        wait_prior_grid();
-        load_table(kb + NB, Lnext, iznext);
-      }
-      /* into the buffer block b-1 used: every warp has passed its barrier */
+      if (lane >= 32 - TW) wtot[warp * TW + c] = incl;
+      /* the next block's depth-table entries: loaded here, stored to shared
+       * memory at the end of B, so the loads' latency overlaps the barrier */
+      if (param_view && kb == 0) wait_prior_grid();
       const bool more = kb + NB < n;
-      if (more) store_table(buf ^ 1, Lnext, iznext);
+      float4 Lnext[NB / NT];
+      float iznext[NB / NT];
+#pragma unroll
+      for (int q = 0; q < NB / NT; q++) {
+        const int p = tid + q * NT, e = (p % TPC) * U + p / TPC;
+        Lnext[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        iznext[q] = 0.0f;
+        if (kb + NB + e < n) {
+          Lnext[q] = __ldg(zl + kb + NB + e);
+          iznext[q] = __ldg(zi + kb + NB + e);
+        }
+      }
       const bool tile_rest = __syncthreads_and(rest ? 1 : 0) != 0;
 
-      /* Y: the column's minimum after the block (every warp, from all warp
-       * totals: the next block's start) and, where a run may hold an event,
-       * the minimum before each sample and the block's events (B). The
-       * 32/TW lanes of a column read every (32/TW)-th warp's total each,
-       * then combine. */
-      constexpr int Q = 32 / TW;
-      int tot[NW / Q];
-#pragma unroll
-      for (int w0 = 0; w0 < NW; w0 += Q) tot[w0 / Q] = wt[(w0 + lane / TW) * TW + c];
-      int mnext = mstart;
-#pragma unroll
-      for (int q = 0; q < NW / Q; q++) mnext = min(mnext, tot[q]);
-#pragma unroll
-      for (int off = TW; off < 32; off <<= 1)
-        mnext = min(mnext, __shfl_xor_sync(FS_FULL_MASK, mnext, off));
+      /* Y: the minimum before each sample, the block's events (B), and the
+       * next block's depth-table entries */
       /* a run whose rows are all at or below the column's minimum at the
-       * block start holds no event; a warp of such runs skips the prefix */
-      if (__any_sync(FS_FULL_MASK, run < mstart)) {
-        /* the minimum over the earlier warps' totals of column c */
+       * block start holds no event; a warp of such runs skips the prefix,
+       * except the last warp, which records the columns' new minima */
+      if (warp == NW - 1 || __any_sync(FS_FULL_MASK, run < mstart)) {
+        /* the minimum over the earlier warps' totals of column c: the 32/TW
+         * lanes of the column read every (32/TW)-th warp each, then combine */
+        constexpr int Q = 32 / TW;
         int prev = mstart;
 #pragma unroll
         for (int w0 = 0; w0 < NW; w0 += Q)
-          if (w0 + lane / TW < warp) prev = min(prev, tot[w0 / Q]);
+          if (w0 + lane / TW < warp) prev = min(prev, wtot[(w0 + lane / TW) * TW + c]);
 #pragma unroll
         for (int off = TW; off < 32; off <<= 1)
           prev = min(prev, __shfl_xor_sync(FS_FULL_MASK, prev, off));
         if (lane >= TW) prev = min(prev, ex);
+        if (j == TPC - 1) mcol[(par ^ 1) * TW + c] = min(prev, run);
+        if (warp == NW - 1) {
+          const bool z = __all_sync(FS_FULL_MASK, lane < 32 - TW || min(prev, run) == 0);
+          if (lane == 31) scal[3] = z;
+        }
         int cnt = 0;
         if (run < prev) {
           int pv = prev;
@@ -1201,17 +1172,21 @@ __global__ void __launch_bounds__(TW *TPC, (CoopShape<TW, TPC, U>::min_blocks))
           }
         }
       }
-      /* the last block, every column at row 0 (a warp holds every column of
-       * the tile, so the vote agrees across warps), or no event possible in
-       * any later block */
-      const bool all_zero = __all_sync(FS_FULL_MASK, mnext == 0);
-      mstart = mnext;
-      if (!more || all_zero || tile_rest) break;
+      if (more) {
+#pragma unroll
+        for (int q = 0; q < NB / NT; q++) {
+          zt[(par ^ 1) * NB + tid + q * NT] = Lnext[q];
+          zv[(par ^ 1) * NB + tid + q * NT] = iznext[q];
+        }
+      }
+      __syncthreads();
+
+      /* the last block, every column at row 0, or no event possible in any
+       * later block */
+      bool done = !more;
+      if (more) done = scal[3] != 0 || tile_rest;
+      if (done) break;
     }
-    /* the columns' final minima (no later block lowers them); a warp holds
-     * every column of the tile */
-    if (warp == 0) note_sky_rows(P, Vp, c0 + c < W ? mstart : INT_MAX, lane);
-    __syncthreads();
     /* every block's events are listed: colour them into the stage */
     if (cp2)
       colour_list(BoolTag<true>{});

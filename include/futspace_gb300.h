@@ -171,9 +171,7 @@ int32_t fs_num_depths(float distance, const fs_params *params);
 int fs_render_device(fs_ctx *ctx, const fs_map *map, const fs_camera *cam,
                      const fs_params *params, int32_t width, int32_t height,
                      uint32_t *out_dev);
-/* Same into HOST memory `out_host`: renders, then copies the rows below the
- * frame's leading all-sky rows back while the calling thread's OpenMP team
- * writes the sky rows, and waits. */
+/* Same into HOST memory `out_host`: renders, copies the frame back and waits. */
 int fs_render(fs_ctx *ctx, const fs_map *map, const fs_camera *cam, const fs_params *params,
               int32_t width, int32_t height, uint32_t *out_host);
 /* Allocation-free variant of fs_render_device (no counterpart in the
@@ -219,11 +217,11 @@ int fs_plan_download(fs_plan *plan, uint32_t *host);
 /* Renders every view and writes every frame to `host` (the fs_plan_download
  * layout), with the views split into `groups` contiguous groups of about equal
  * pixel count (1..16): group g+1 renders while group g's frames are copied, so
- * with pinned host memory the copy time mostly hides the render time. The
- * render kernels also find, per view, the rows at the top that are sky in every
- * column (above every column's highest terrain row); only the rows below them
- * are copied, and the calling thread's OpenMP team writes the sky rows into
- * `host` meanwhile (the same pixels as a full copy). Waits for the copies. */
+ * with pinned host memory the copy time mostly hides the render time. A small
+ * kernel after each group's render finds, per view, the leading rows that hold
+ * nothing but the sky value; only the rows below them are copied, and the
+ * calling thread's OpenMP team writes the sky rows into `host` meanwhile (the
+ * same pixels as a full copy). Waits for the copies. */
 int fs_plan_run_download(fs_plan *plan, uint32_t *host, int32_t groups);
 /* Bytes of the last fs_plan_run_download: copied device to host (frame rows
  * and the per-view sky row counts) and written on the host (sky rows). */
