@@ -632,7 +632,11 @@ int fs_plan_run_download(fs_plan *p, uint32_t *host, int32_t groups) {
     if (!e) filled += fill_sky_rows(p, host, v0, v1);
   }
   if (!e) e = cudaStreamSynchronize(p->copy_stream);
-  if (e) return fs_cuda_fail(ctx, e, "pipelined render and download");
+  if (e) {
+    /* no copy into the caller's buffer outlives the call */
+    cudaStreamSynchronize(p->copy_stream);
+    return fs_cuda_fail(ctx, e, "pipelined render and download");
+  }
   p->dl_copied = copied;
   p->dl_filled = filled;
   return FS_OK;
