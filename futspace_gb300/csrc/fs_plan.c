@@ -11,6 +11,8 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <omp.h>
+
 #include "fs_internal.h"
 #include "fs_priv.h"
 
@@ -573,13 +575,18 @@ int fs_plan_run_download(fs_plan *p, uint32_t *host, int32_t groups) {
     rc = plan_build_groups(p, groups);
     if (rc) return rc;
   }
+  /* the host writes the sky rows when its OpenMP team can outrun the link (one
+   * thread writes about 44 GB/s, the link moves 193); a smaller team (e.g.
+   * OMP_NUM_THREADS=1) gets whole frames over the link, a copy per group */
+  const int host_sky = omp_get_max_threads() >= 4;
   int32_t max_n = 0;
   for (int v = 0; v < p->nviews; v++)
     if (p->ncap[v] > max_n) max_n = p->ncap[v];
   int e = cudaMemsetAsync(p->grp_heads_d, 0, sizeof(int32_t) * (size_t)groups, ctx->stream);
   if (!e) e = cudaMemsetAsync(p->head_d, 0, 2 * sizeof(int32_t), ctx->stream);
   /* every view's all-sky row count starts above any frame height */
-  if (!e) e = cudaMemsetAsync(p->sky_d, 0x7F, sizeof(int32_t) * (size_t)p->nviews, ctx->stream);
+  if (!e && host_sky)
+    e = cudaMemsetAsync(p->sky_d, 0x7F, sizeof(int32_t) * (size_t)p->nviews, ctx->stream);
   if (!e) e = fsk_ztable(p->fv_d, NULL, p->nviews, max_n, p->zline, p->zinvz, ctx->stream);
   if (!e) e = plan_segmin(p);
   const int32_t per_cta = fsk_items_per_cta(&p->tune);
@@ -599,22 +606,34 @@ int fs_plan_run_download(fs_plan *p, uint32_t *host, int32_t groups) {
                       p->wmax, ctx->stream);
     const int32_t v0 = p->grp_first[g], v1 = p->grp_first[g + 1];
     /* each finished frame's leading rows that hold nothing but sky */
-    if (!e)
+    if (!e && host_sky)
       e = fsk_sky_rows(p->fv_d + v0, NULL, v1 - v0, p->stride_max, p->sky_d + v0, ctx->stream);
     if (!e) e = cudaEventRecord(p->grp_done[g], ctx->stream);
-    if (!e) e = cudaStreamWaitEvent(p->meta_stream, p->grp_done[g], 0);
-    if (!e)
-      e = cudaMemcpyAsync(p->sky_h + v0, p->sky_d + v0, sizeof(int32_t) * (size_t)(v1 - v0),
-                          cudaMemcpyDeviceToHost, p->meta_stream);
-    if (!e) e = cudaEventRecord(p->grp_meta[g], p->meta_stream);
+    if (!e && host_sky) {
+      e = cudaStreamWaitEvent(p->meta_stream, p->grp_done[g], 0);
+      if (!e)
+        e = cudaMemcpyAsync(p->sky_h + v0, p->sky_d + v0, sizeof(int32_t) * (size_t)(v1 - v0),
+                            cudaMemcpyDeviceToHost, p->meta_stream);
+      if (!e) e = cudaEventRecord(p->grp_meta[g], p->meta_stream);
+    }
   }
-  ctx->launches += 1 + 2 * groups + (p->nsegitems ? 1 : 0) + (p->segbuf_d ? groups : 0);
+  ctx->launches += 1 + (host_sky ? 2 : 1) * groups + (p->nsegitems ? 1 : 0) +
+                   (p->segbuf_d ? groups : 0);
   /* per group, once its sky rows are known: the rows below them cross the
    * link (one copy per view, after the group's render), and the host's
    * threads write the sky rows meanwhile */
-  int64_t copied = 4 * (int64_t)p->nviews, filled = 0;
+  int64_t copied = host_sky ? 4 * (int64_t)p->nviews : 0, filled = 0;
   for (int g = 0; !e && g < groups; g++) {
     const int32_t v0 = p->grp_first[g], v1 = p->grp_first[g + 1];
+    if (!host_sky) {
+      const int64_t a = p->offsets[v0], b = v1 < p->nviews ? p->offsets[v1] : p->total_px;
+      e = cudaStreamWaitEvent(p->copy_stream, p->grp_done[g], 0);
+      if (!e && b > a)
+        e = cudaMemcpyAsync(host + a, p->frames + a, sizeof(uint32_t) * (size_t)(b - a),
+                            cudaMemcpyDeviceToHost, p->copy_stream);
+      copied += 4 * (b - a);
+      continue;
+    }
     e = cudaEventSynchronize(p->grp_meta[g]);
     if (!e) e = cudaStreamWaitEvent(p->copy_stream, p->grp_done[g], 0);
     for (int32_t v = v0; !e && v < v1; v++) {

@@ -221,7 +221,8 @@ int fs_plan_download(fs_plan *plan, uint32_t *host);
  * kernel after each group's render finds, per view, the leading rows that hold
  * nothing but the sky value; only the rows below them are copied, and the
  * calling thread's OpenMP team writes the sky rows into `host` meanwhile (the
- * same pixels as a full copy). Waits for the copies. */
+ * same pixels as a full copy). A team of fewer than 4 threads (e.g.
+ * OMP_NUM_THREADS=1) gets whole frames copied instead. Waits for the copies. */
 int fs_plan_run_download(fs_plan *plan, uint32_t *host, int32_t groups);
 /* Bytes of the last fs_plan_run_download: copied device to host (frame rows
  * and the per-view sky row counts) and written on the host (sky rows). */

@@ -1,5 +1,7 @@
 """GPU parity: every frame the CUDA path renders equals the CPU oracle's, bit
 for bit (ARGB u32 output: no tolerance). All calls go through the C ABI."""
+import os
+
 import numpy as np
 import pytest
 
@@ -153,6 +155,42 @@ def test_run_download_sky_rows(fs, orc, gpu_ctx, maps256):
         assert count_diff(plan.frames(plan.run_download(out, groups=1))[0], ref) == 0, tune
     plan.close()
     fmap.close()
+
+
+def test_run_download_small_host_team(tmp_path):
+    """With OMP_NUM_THREADS=1 the download copies whole frames (no host-written
+    sky rows): same frames as the oracle, byte counters of a whole copy."""
+    import subprocess
+    import sys
+    from pathlib import Path
+
+    root = Path(__file__).resolve().parent.parent
+    script = tmp_path / "small_team.py"
+    script.write_text(f"""
+import sys
+sys.path.insert(0, {str(root)!r})
+import numpy as np
+import futspace_gb300 as fs, oracle
+ctx = fs.Context(0)
+hm = fs.gen_heights(21, 256, 0.55); cm = fs.gen_colors(22, hm, 12)
+fmap = fs.Map(ctx, hm, cm)
+cams = fs.gen_cameras(501, hm, 4, above=(20, 80), distance=(300, 900), screen_h=96)
+views = [(c, 128, 96) for c in cams]
+plan = fs.Plan(ctx, [fmap], views)
+out = np.full(plan.total_pixels, 5, np.uint32)
+frames = plan.frames(plan.run_download(out, groups=2))
+p = oracle.make_params()
+bad = sum(int(np.count_nonzero(f != oracle.render(c, p, hm, cm, 128, 96, threads=1)))
+          for f, (c, w, h) in zip(frames, views))
+copied, filled = plan.download_bytes()
+assert bad == 0, bad
+assert filled == 0 and copied == 4 * plan.total_pixels, (copied, filled)
+print("ok")
+""")
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    r = subprocess.run([sys.executable, str(script)], capture_output=True, text=True, env=env,
+                       timeout=600)
+    assert r.returncode == 0 and "ok" in r.stdout, r.stdout + r.stderr
 
 
 def test_batch_two_maps_and_camera_update(fs, orc, gpu_ctx, maps1024, maps256):
