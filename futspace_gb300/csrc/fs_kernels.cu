@@ -175,24 +175,11 @@ __global__ void sky_rows_kernel(const FsView *views, FsView view0, int32_t *out)
   const uint32_t *f = V.out + (size_t)r0 * W;
   const int n = (r1 - r0) * W;
   int first = INT_MAX;
-  if ((W & 3) == 0 && ((uintptr_t)f & 15) == 0) {
-    /* rows of whole 16-byte groups: four pixels per load */
-    const uint4 *f4 = reinterpret_cast<const uint4 *>(f);
-    for (int i = threadIdx.x; i < n / 4; i += blockDim.x) {
-      const uint4 q = __ldcs(f4 + i);
-      if (q.x != sky || q.y != sky || q.z != sky || q.w != sky) {
-        const int j = q.x != sky ? 0 : (q.y != sky ? 1 : (q.z != sky ? 2 : 3));
-        first = r0 + (4 * i + j) / W;
-        break;
-      }
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+    if (__ldcs(f + i) != sky) {
+      first = r0 + i / W;
+      break;
     }
-  } else {
-    for (int i = threadIdx.x; i < n; i += blockDim.x)
-      if (__ldcs(f + i) != sky) {
-        first = r0 + i / W;
-        break;
-      }
-  }
   first = (int)__reduce_min_sync(0xffffffffu, (unsigned)first);
   if ((threadIdx.x & 31) == 0 && first != INT_MAX) atomicMin(slot, first);
 }
